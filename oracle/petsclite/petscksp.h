@@ -1,0 +1,2 @@
+/* petsclite: everything lives in petsc.h */
+#include "petsc.h"
