@@ -1,0 +1,291 @@
+"""Benchmark of the GB300 SEM time loop: DOF-updates/s.
+
+Default workload: the 2048 x 2048-element, degree-4 heterogeneous solve (20 km
+square, Gaussian-random-field Vp, 64 receivers; 67.1M GLL nodes, 134.3M DOF),
+one GPU, FP32 with Kahan-compensated updates as the headline, FP64 (reference
+operation order) measured beside it.  A "step" is one explicit time step of the
+whole mesh (the loop body of se2wave.c:4722-4775).  The state (5.4 GB in FP32+
+Kahan, 6.4 GB in FP64) is far larger than L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm on the host cores (the oracle
+port, bit-identical to se2wave.c compiled in place) on a bounded sample of the
+same workload, one independent solve per host thread.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DOF-updates/s"
+ALG_BYTES_NOTE = "per node-step: read+write of the fields, lumped mass, cell Lame pair"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def alg_bytes_per_node(precision: str, ne: int, nnodes: int) -> float:
+    """Algorithmic DRAM bytes per node per step (unique traffic only)."""
+    cell = ne / nnodes
+    if precision == "fp64":
+        return 2 * 3 * 16 + 8 + 16 * cell          # u,v,a (double2) in+out, M, (lambda, mu)
+    if precision == "fp32_kahan":
+        return 2 * 5 * 8 + 4 + 8 * cell            # u,v,a,cu,cv (float2) in+out, 1/M, (lambda, mu)
+    return 2 * 3 * 8 + 4 + 8 * cell
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(threads: int, rows: int, steps: int, warmup: int = 1):
+    """The oracle port (the reference algorithm) on host threads: each thread an
+    independent solve of a 2048 x `rows` element strip of the workload."""
+    from oracle import oracle as O
+    from se2dr_fork_gb300 import spec as S
+    from se2dr_fork_gb300 import host as H
+    vp = H.gaussian_random_field(2048, rows, 5000.0, 0.1, 8.0, seed=2048)
+    sp = S.grf2048(2048, rows, nt=warmup + steps + 2, cells=(vp, vp / 1.73, np.full_like(vp, 2700.0)))
+    # same element shape as the full workload: the strip is rows/2048 of its height
+    h = 20000.0 * rows / 2048.0
+    sp = sp.replace(scale=(20000.0, h), shift=(-10000.0, -h / 2), receivers=[(x, 0.0) for x, _ in sp.receivers])
+    secs = O.bench(sp, threads, warmup, steps, record=True)
+    dof = sp.ndof
+    return {"value": threads * dof * steps / secs, "seconds": secs, "dof_per_thread": dof,
+            "sample": f"{threads} independent solves of a 2048x{rows}-element strip of the workload "
+                      f"(degree 4, {dof} DOF each, receivers recorded), {steps} steps after {warmup} warm-up"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    # calibrate the strip so the whole run stays within ~3 minutes
+    probe = cpu_baseline(threads, 8, 1, 0)
+    per_row = probe["seconds"] / 8.0
+    budget = 150.0 / max(1, args.steps + args.warmup)
+    rows = int(max(1, min(64, budget / max(per_row, 1e-6))))
+    res = cpu_baseline(threads, rows, args.steps, args.warmup)
+    line = {"impl": "reference", "metric": METRIC, "value": res["value"], "unit": "DOF/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * res["seconds"] / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "grf2048: 2048x2048 elements, degree 4, 20 km square, GRF Vp, 64 receivers",
+                       "sample": res["sample"], "host_threads": threads},
+            "cpu_baseline": {"value": res["value"], "unit": "DOF/s", "cores": threads, "kind": "port",
+                             "sample": res["sample"]},
+            "e2e": {"value": res["value"], "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def time_steps(sol, steps, warmup, stream, torch):
+    """Device time of `steps` steps (CUDA events on the launching stream)."""
+    sol.advance(warmup)
+    sol.traces()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    launches0 = sol.info()["launches"]
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    sol.advance(steps)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    launches = sol.info()["launches"] - launches0
+    sol.traces()
+    return ev0.elapsed_time(ev1) / 1e3, launches
+
+
+def run_ours(args, rank, world):
+    import torch
+    from se2dr_fork_gb300 import gpu as G
+    from se2dr_fork_gb300 import host as H
+    from se2dr_fork_gb300 import spec as S
+
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def tmax(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    spec = S.grf2048(args.mx, args.mx, p=4, nt=args.steps + args.warmup + 10)
+    setup = H.Setup(spec)
+    nnodes, ne = setup.nnodes, setup.mx * setup.my
+    dof = 2 * nnodes
+    stream = torch.cuda.Stream()
+    hbm, peak_kind = peaks()
+    results = {}
+    for prec in [args.precision] + (["fp64"] if args.precision != "fp64" and not args.no_fp64 else []):
+        k = args.steps if prec == args.precision else max(3, args.steps // 8)
+        sol = G.Solver(setup, prec, trace_capacity=k + args.warmup + 2)
+        sol.set_stream(stream.cuda_stream)
+        barrier()
+        with ClockSampler(local) as clk:
+            secs, launches = time_steps(sol, k, args.warmup, stream, torch)
+        secs = tmax(secs)
+        sol.close()
+        per = secs / k
+        b = alg_bytes_per_node(prec, ne, nnodes)
+        achieved = b * nnodes / per / 1e9
+        results[prec] = {"value": world * dof * k / secs, "ms_per_step": 1e3 * per, "steps": k,
+                         "launches": launches, "clocks": clk.summary(),
+                         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                                      "frac": achieved / hbm, "traffic": None,
+                                      "alg_bytes_per_node": b, "peak_kind": peak_kind}}
+
+    # end to end through the C-ABI: create (upload from host) + K steps + traces read back + destroy
+    prec = args.precision
+    barrier()
+    t0 = time.perf_counter()
+    sol = G.Solver(setup, prec, trace_capacity=args.steps + 2)
+    sol.advance(args.steps)
+    tr = sol.traces()
+    sol.close()
+    torch.cuda.synchronize()
+    e2e_s = tmax(time.perf_counter() - t0)
+    tsize = 8 if prec == "fp64" else 4
+    h2d = (nnodes * tsize + 2 * ne * tsize + 4 * (setup.mx + setup.my) * tsize + 2 * setup.npe * (tsize + 8)
+           + setup.nsrc * 2 * setup.npe * tsize + 12 * setup.nrec + 8 * setup.nsrc * args.steps)
+    d2h = tr.shape[0] * 7 * setup.nrec * 8
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    head = results[args.precision]
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        c = cpu_baseline(threads, args.cpu_rows, args.cpu_steps)
+        cpu = {"value": c["value"], "unit": "DOF/s", "cores": threads, "kind": "port", "sample": c["sample"]}
+        try:
+            c1 = cpu_baseline(1, args.cpu_rows, max(2, args.cpu_steps // 2))
+            cpu["single_core_value"] = c1["value"]
+        except Exception:
+            pass
+    line = {"metric": METRIC, "value": head["value"], "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if prec != "fp64" else "f64", "data": "synthetic",
+            "config": {"workload": f"grf2048: {args.mx}x{args.mx} elements, degree 4, 20 km square, "
+                                   f"Gaussian-random-field Vp (mean 5000, 10% std, corr 8 cells), Vp/Vs 1.73, "
+                                   f"rho 2700, explosive Ricker f0 8 Hz, 64 receivers",
+                       "precision": prec, "nodes": nnodes, "dof": dof, "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (state %.1f GB)" % ((10 if prec == "fp32_kahan" else 6)
+                                                                       * nnodes * (4 if prec != 'fp64' else 8) * 2 / 1e9)},
+            "roofline": head["roofline"], "clocks": head["clocks"], "gpu_launches": head["launches"],
+            "e2e": {"value": world * dof * args.steps / e2e_s, "unit": "DOF/s", "h2d_bytes_per_step": h2d / args.steps,
+                    "d2h_bytes_per_step": d2h / args.steps, "seconds": e2e_s,
+                    "includes": "se2gpu_create (upload of the set-up from host memory), advance, traces, destroy"},
+            "cpu_baseline": cpu}
+    if "fp64" in results and args.precision != "fp64":
+        r = results["fp64"]
+        line["fp64"] = {"value": r["value"], "ms_per_step": r["ms_per_step"], "steps": r["steps"],
+                        "roofline": r["roofline"], "clocks": r["clocks"]}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", choices=["fp32_kahan", "fp32", "fp64"], default="fp32_kahan")
+    ap.add_argument("--mx", type=int, default=2048, help="elements per side (default: the 2048^2 workload)")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-rows", type=int, default=32)
+    ap.add_argument("--cpu-steps", type=int, default=6)
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

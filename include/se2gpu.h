@@ -1,0 +1,114 @@
+/*
+ * se2gpu.h -- C-ABI of the GB300 (sm_103a) SEM time-loop library, libse2gpu.so.
+ *
+ * Drop-in boundary for the hot path of Nicolucas/se2dr_fork se2wave.c.  The
+ * reference has no plugin or FFI layer: its boundary is the C function
+ *   PetscErrorCode AssembleLinearForm_ElastoDynamics2d(SpecFECtx c, Vec u, Vec F)   (se2wave.c:1285)
+ * plus the Vec operations of the time loop (se2wave.c:4722-4775) that surround
+ * it.  This header replaces them:
+ *
+ *   se2gpu_assemble_linear_form   <- AssembleLinearForm_ElastoDynamics2d           (se2wave.c:1285-1429)
+ *   se2gpu_advance                <- one pass of the loop body per step:
+ *                                    VecAXPY x3 (4726-4730), SeismicSourceEvaluate (4733, 3470-3497),
+ *                                    AssembleLinearForm_ElastoDynamics2d (4736), VecAXPY(f,1,g) (4739),
+ *                                    VecPointwiseDivide (4742), VecAXPY (4745), and the per-step
+ *                                    receiver sampling of RecordUVA_MultipleStations_NearestGLL_MPI
+ *                                    (2886-2981)
+ *   se2gpu_norms                  <- VecNorm/VecMin/VecMax of u and v (4747-4755)
+ *   se2gpu_set_fields/get_fields  <- the u, v, a Vecs (DMCreateGlobalVector, 4594-4596)
+ *
+ * Conventions (mirroring PetscErrorCode): every call returns 0 on success and a
+ * negative code on error; se2gpu_last_error() returns the handle's message.  No
+ * exception crosses the ABI.  The library owns all device memory; the caller
+ * owns host arrays.  One host thread per handle.  Vectors are interleaved
+ * [node][component] with node = i + j*(p*mx+1), exactly the reference's Vec
+ * layout, so fields move between the two unchanged.
+ */
+#ifndef SE2GPU_H
+#define SE2GPU_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* precision modes */
+#define SE2GPU_FP64        64  /* FP64, reference operation order, no fused multiply-add: bit-identical to the CPU reference */
+#define SE2GPU_FP32_KAHAN  33  /* FP32 arithmetic, Kahan-compensated u and v updates */
+#define SE2GPU_FP32        32  /* FP32 arithmetic, plain updates */
+
+/* error codes */
+#define SE2GPU_OK            0
+#define SE2GPU_ERR_ARG      -1  /* invalid argument */
+#define SE2GPU_ERR_CUDA     -2  /* CUDA runtime error */
+#define SE2GPU_ERR_NOMEM    -3  /* device allocation failed */
+#define SE2GPU_ERR_STATE    -4  /* call not valid in the handle's state */
+#define SE2GPU_ERR_NUMERIC  -5  /* non-finite value detected */
+
+/* The discrete problem, produced by the FP64 host set-up (se2host.h).  All
+   pointers are host memory, read during se2gpu_create only. */
+typedef struct se2gpu_problem {
+  int mx, my, p;             /* elements in x and y, polynomial degree 1..8 */
+  double dt;                 /* time step */
+  const double *D;           /* (p+1)^2: D[q*(p+1)+i] = dN_i/dxi at GLL point q */
+  const double *wq;          /* (p+1)^2: tensor GLL weights w[i+j*(p+1)] */
+  const double *J00, *J11;   /* mx, my: element half-widths */
+  const double *iJ00, *iJ11; /* mx, my: their reciprocals */
+  const double *lambda, *mu; /* mx*my cell Lame parameters */
+  const double *mass;        /* (p*mx+1)*(p*my+1) lumped mass per node */
+  int nsrc;
+  const int *src_elem;       /* nsrc owning elements */
+  const double *src_vals;    /* nsrc*2*(p+1)^2 element values, [2*k + component] */
+  int nrec;
+  const int *rec_node;       /* nrec nearest GLL node */
+  const int *rec_elem;       /* nrec owning element */
+  const int *rec_gll;        /* nrec element-local GLL index of that node */
+} se2gpu_problem;
+
+typedef struct se2gpu_solver se2gpu_solver;
+
+/* Allocate and upload a problem.  trace_capacity = receiver rows buffered on
+   the device between se2gpu_traces calls.  The fields start at zero. */
+int  se2gpu_create(const se2gpu_problem *prob, int precision, int trace_capacity, se2gpu_solver **out);
+void se2gpu_destroy(se2gpu_solver *h);
+const char *se2gpu_last_error(const se2gpu_solver *h);
+/* message of the last se2gpu_create failure in this thread (no handle exists then) */
+const char *se2gpu_create_error(void);
+
+/* Launch on this CUDA stream (a cudaStream_t; NULL = the handle's own stream). */
+int se2gpu_set_stream(se2gpu_solver *h, void *stream);
+int se2gpu_synchronize(se2gpu_solver *h);
+
+/* Fields as FP64 host arrays of 2*nnodes (any may be NULL). */
+int se2gpu_set_fields(se2gpu_solver *h, const double *u, const double *v, const double *a);
+int se2gpu_get_fields(se2gpu_solver *h, double *u, double *v, double *a);
+
+/* Advance nsteps steps.  stf[k*nsrc + s] is source s's source-time function at
+   the time of step k (the host evaluates the STF objects, as the reference does
+   per step).  One receiver row per step is buffered on the device; the call
+   fails with SE2GPU_ERR_STATE when the trace buffer would overflow. */
+int se2gpu_advance(se2gpu_solver *h, int nsteps, const double *stf);
+
+/* Copy up to max_rows buffered receiver rows (oldest first) into out[row][7*nrec]
+   = (ux uy vx vy ax ay curl(v)) per receiver, FP64, and empty the buffer.
+   Returns the number of rows copied (>= 0) or an error code. */
+int se2gpu_traces(se2gpu_solver *h, double *out, int max_rows);
+
+/* out[6] = max, min, l2 of u then of v (VecMax/VecMin/VecNorm NORM_2). */
+int se2gpu_norms(se2gpu_solver *h, double out[6]);
+
+/* F = AssembleLinearForm_ElastoDynamics2d(u): internal force of the
+   displacement u (2*nnodes FP64 host arrays).  Does not touch the fields. */
+int se2gpu_assemble_linear_form(se2gpu_solver *h, const double *u, double *F);
+
+/* Same on device arrays of the handle's precision (double or float, 2*nnodes),
+   launched on the handle's stream, no synchronisation. */
+int se2gpu_assemble_linear_form_device(se2gpu_solver *h, const void *u_dev, void *F_dev);
+
+/* Introspection: ints[0..7] = nx_g, ny_g, p, precision, nsrc, nrec, kernel
+   launches so far, buffered trace rows; device pointers of the current u, v, a. */
+int se2gpu_info(const se2gpu_solver *h, long *ints);
+int se2gpu_device_fields(const se2gpu_solver *h, void **u, void **v, void **a);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,107 @@
+/*
+ * se2host.h -- FP64 host set-up for the GB300 SEM time loop (C-ABI).
+ *
+ * The host side of se2wave stays in C: everything here runs once per problem on
+ * the CPU in double precision and produces the small tables and per-node arrays
+ * that the device library (se2gpu.h) consumes.  Each function states the
+ * reference routine of Nicolucas/se2dr_fork se2wave.c it replaces; values are
+ * identical to the reference's bit for bit (same operation order, no fused
+ * multiply-add).
+ *
+ * Error convention (mirrors PetscErrorCode): 0 = success, < 0 = error, message
+ * available from se2_host_last_error() (thread-local).
+ */
+#ifndef SE2HOST_H
+#define SE2HOST_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SE2_STF_RICKER   0   /* (t0, f0, amp)          se2wave.c:3500-3545 */
+#define SE2_STF_GAUSSIAN 1   /* (t0, omega, amp)       se2wave.c:3548-3590 */
+#define SE2_STF_YOFFE    2   /* (tau_S, tau_R, D_max)  se2wave.c:3592-3822 */
+
+/* Problem specification: what se2wave_demo (se2wave.c:4541-4807) hard-codes or
+   reads from -mx -my -bdegree -tmax -dt -nt. */
+typedef struct se2_spec {
+  int mx, my, p;                 /* -mx -my -bdegree */
+  double scale[2], shift[2];     /* [0,1]^2 scaled then shifted (SpecFECtxScaleMeshCoords, 781-823) */
+  const double *cell_vp, *cell_vs, *cell_rho; /* per cell, mx*my each, or NULL for the constants */
+  double vp, vs, rho;            /* SpecFECtxSetConstantMaterialProperties_Velocity (1161-1175) */
+  double cfl;                    /* factor on the CFL step; the demo uses 0.5 (4709) */
+  double dt;                     /* > 0: -dt */
+  double tmax;                   /* -tmax */
+  int nt;                        /* >= 0: -nt, else (int)(tmax/dt)+4 (4714) */
+  int nearest_internal_gll;      /* -use_nearest_internal_gll (3125) */
+  int nsrc;
+  const double *src_xy;          /* nsrc*2 */
+  const double *src_m;           /* nsrc*4: [M00 M01 M10 M11] */
+  const int *stf_type;           /* nsrc: SE2_STF_* */
+  const double *stf_par;         /* nsrc*3 */
+  int nrec;
+  const double *rec_xy;          /* nrec*2 */
+} se2_spec;
+
+/* Everything the device needs, FP64, owned by the library. */
+typedef struct se2_setup {
+  int mx, my, p, n1, npe, nx_g, ny_g;
+  long nnodes;
+  double *xi;        /* n1 GLL nodes, ascending (CreateGLLCoordsWeights 103-209) */
+  double *w1d;       /* n1 GLL weights in the reference's order */
+  double *wq;        /* npe tensor weights w[i+j*n1] = w1d[i]*w1d[j] (861-865) */
+  double *D;         /* n1*n1: D[q*n1+i] = dN_i/dxi at xi_q (TabulateBasisDerivatives1d_CLEGENDRE 387-523) */
+  double *xnode;     /* nx_g node x-coordinates (the mesh is a tensor product, 739-823) */
+  double *ynode;     /* ny_g node y-coordinates */
+  double *J00, *J11; /* mx, my: half element widths 0.5*dx (1245-1251) */
+  double *iJ00, *iJ11; /* 1.0/J00, 1.0/J11 (1270-1271) */
+  double *lambda, *mu, *rho; /* mx*my cell data (29-33) */
+  double *mass;      /* nnodes lumped mass, ascending-element sum (AssembleBilinearForm_Mass2d 1431-1498) */
+  double gmin[2], gmax[2];   /* DMGetBoundingBox */
+  double dt_cfl;     /* ElastoDynamicsComputeTimeStep_2d (2276-2349) */
+  double dt, tmax;
+  long nt;           /* step bound */
+  long nsteps;       /* steps the loop of se2wave.c:4722-4775 takes (stops when time >= tmax) */
+  int nsrc;
+  int *src_elem, *src_gll;   /* owning element, closest interior GLL (2995-3243) */
+  double *src_vals;  /* nsrc*2*npe element values [2*k+c] (SeismicSourceSetup_Moment_Pointwise 3367-3429) */
+  int *stf_type;
+  double *stf_par;
+  int nrec;
+  double *rec_xy;
+  int *rec_node, *rec_elem, *rec_gll; /* nearest GLL node (RecordUVA_MultipleStations_NearestGLL_MPI 2700-2810) */
+} se2_setup;
+
+const char *se2_host_last_error(void);
+
+/* Full set-up (replaces SpecFECtxCreateMesh + ScaleMeshCoords + material +
+   AssembleBilinearForm_Mass2d + SeismicSourceCreate/Setup + receiver location +
+   ElastoDynamicsComputeTimeStep_2d). */
+int  se2_setup_create(const se2_spec *spec, se2_setup **out);
+void se2_setup_destroy(se2_setup *s);
+
+/* CreateGLLCoordsWeights (se2wave.c:103-209): xi ascending, w in the reference's order */
+int se2_gll(int p, double *xi, double *w);
+/* TabulateBasis1d_CLEGENDRE (253-385): N[k*(p+1)+i] = N_i(x_k) */
+int se2_basis_1d(int p, int npoints, const double *x, double *N);
+/* TabulateBasisDerivatives1d_CLEGENDRE (387-523): dN[k*(p+1)+i] = dN_i/dxi(x_k) */
+int se2_basis_deriv_1d(int p, int npoints, const double *x, double *dN);
+
+/* Source-time function values (SeismicSTFEvaluate 3458-3466 with the Ricker,
+   Gaussian and Yoffe evaluators).  For steps k = 1..n after time `*time`, the
+   time is advanced as time = time + dt (se2wave.c:4724) and times[k-1] and
+   stf[(k-1)*nsrc + s] are written; *time is left at the last step's time. */
+int se2_stf_block(const se2_setup *s, double *time, long n, double *times, double *stf);
+/* one STF at one time */
+int se2_stf_eval(int type, const double par[3], double time, double *value);
+
+/* Seeded Gaussian random field on the mx*my cell grid (row-major, x fastest):
+   mean*(1 + rel_std*z), z ~ N(0,1) white noise (splitmix64 + Box-Muller)
+   smoothed by a separable Gaussian of std corr_cells (periodic), renormalised
+   to unit variance and clipped to +-3. */
+int se2_gaussian_random_field(int mx, int my, double mean, double rel_std, double corr_cells,
+                              unsigned long long seed, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

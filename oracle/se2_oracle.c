@@ -635,7 +635,11 @@ int se2o_create(const se2o_spec *sp, se2o_ctx **out)
   c->dt = c->dt_cfl * sp->cfl;
   if (sp->dt > 0.0) c->dt = sp->dt;
   c->tmax = sp->tmax;
-  c->nt = (long)(int)(c->tmax / c->dt) + 4;
+  {
+    /* (PetscInt)(tmax/dt)+4, saturated where the reference's conversion would overflow */
+    double q = c->tmax / c->dt;
+    c->nt = (q < 2147483000.0) ? (long)(int)q + 4 : 2147483647L;
+  }
   if (sp->nt >= 0) c->nt = sp->nt;
   c->time = 0.0;
   c->k = 0;

@@ -1,0 +1,209 @@
+"""ctypes binding of the GB300 time-loop library (include/se2gpu.h, lib/libse2gpu.so).
+
+This is the only compute path of the package: there is no CPU fallback.  If the
+library is missing or no GPU is present, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+from .host import Setup
+
+_LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libse2gpu.so")
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+FP64, FP32_KAHAN, FP32 = 64, 33, 32
+PRECISIONS = {"fp64": FP64, "fp32_kahan": FP32_KAHAN, "fp32": FP32}
+
+# symbols declared in include/se2gpu.h
+EXPORTS = ["se2gpu_create", "se2gpu_destroy", "se2gpu_last_error", "se2gpu_create_error", "se2gpu_set_stream",
+           "se2gpu_synchronize", "se2gpu_set_fields", "se2gpu_get_fields", "se2gpu_advance", "se2gpu_traces",
+           "se2gpu_norms", "se2gpu_assemble_linear_form", "se2gpu_assemble_linear_form_device", "se2gpu_info",
+           "se2gpu_device_fields"]
+
+
+class _CProblem(C.Structure):
+    _fields_ = [("mx", C.c_int), ("my", C.c_int), ("p", C.c_int), ("dt", C.c_double),
+                ("D", _dp), ("wq", _dp), ("J00", _dp), ("J11", _dp), ("iJ00", _dp), ("iJ11", _dp),
+                ("lambda_", _dp), ("mu", _dp), ("mass", _dp),
+                ("nsrc", C.c_int), ("src_elem", _ip), ("src_vals", _dp),
+                ("nrec", C.c_int), ("rec_node", _ip), ("rec_elem", _ip), ("rec_gll", _ip)]
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            raise RuntimeError(f"{_LIB_PATH} is missing: the CUDA library must be built (__graft_entry__.build())")
+        L = C.CDLL(_LIB_PATH)
+        vp = C.c_void_p
+        L.se2gpu_create.argtypes = [C.POINTER(_CProblem), C.c_int, C.c_int, C.POINTER(vp)]
+        L.se2gpu_destroy.argtypes = [vp]
+        L.se2gpu_destroy.restype = None
+        L.se2gpu_last_error.argtypes = [vp]
+        L.se2gpu_last_error.restype = C.c_char_p
+        L.se2gpu_create_error.restype = C.c_char_p
+        L.se2gpu_set_stream.argtypes = [vp, vp]
+        L.se2gpu_synchronize.argtypes = [vp]
+        L.se2gpu_set_fields.argtypes = [vp, _dp, _dp, _dp]
+        L.se2gpu_get_fields.argtypes = [vp, _dp, _dp, _dp]
+        L.se2gpu_advance.argtypes = [vp, C.c_int, _dp]
+        L.se2gpu_traces.argtypes = [vp, _dp, C.c_int]
+        L.se2gpu_norms.argtypes = [vp, _dp]
+        L.se2gpu_assemble_linear_form.argtypes = [vp, _dp, _dp]
+        L.se2gpu_assemble_linear_form_device.argtypes = [vp, vp, vp]
+        L.se2gpu_info.argtypes = [vp, C.POINTER(C.c_long)]
+        L.se2gpu_device_fields.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]
+        _lib = L
+    return _lib
+
+
+def _p(a: Optional[np.ndarray], t=_dp):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+class GpuError(RuntimeError):
+    pass
+
+
+class Solver:
+    """One problem resident on the GPU, advanced by the fused sm_103a step kernel.
+
+    Mirrors the reference driver: ``advance`` runs the body of the time loop of
+    se2wave.c:4722-4775 for n steps, evaluating the source-time functions on the
+    host per step as the reference does; ``traces`` returns the per-step
+    receiver rows of RecordUVA_MultipleStations_NearestGLL (time first).
+    """
+
+    def __init__(self, setup: Setup, precision="fp64", trace_capacity: Optional[int] = None):
+        self.setup = setup
+        self.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        s = setup
+        self._keep = [np.ascontiguousarray(x) for x in (s.D.reshape(-1), s.wq, s.J00, s.J11, s.iJ00, s.iJ11,
+                                                       s.lam, s.mu, s.mass, s.src_elem, s.src_vals.reshape(-1),
+                                                       s.rec_node, s.rec_elem, s.rec_gll)]
+        (D, wq, J00, J11, iJ00, iJ11, lam, mu, mass, se, sv, rn, re, rg) = self._keep
+        pr = _CProblem(mx=s.mx, my=s.my, p=s.p, dt=s.dt, D=_p(D), wq=_p(wq), J00=_p(J00), J11=_p(J11),
+                       iJ00=_p(iJ00), iJ11=_p(iJ11), lambda_=_p(lam), mu=_p(mu), mass=_p(mass),
+                       nsrc=s.nsrc, src_elem=_p(se, _ip), src_vals=_p(sv),
+                       nrec=s.nrec, rec_node=_p(rn, _ip), rec_elem=_p(re, _ip), rec_gll=_p(rg, _ip))
+        if trace_capacity is None:
+            trace_capacity = max(1, min(s.nsteps, 1 << 16)) if s.nrec else 0
+        self.trace_capacity = int(trace_capacity)
+        h = C.c_void_p()
+        rc = lib().se2gpu_create(C.byref(pr), self.precision, self.trace_capacity, C.byref(h))
+        if rc != 0:
+            raise GpuError(f"se2gpu_create failed ({rc}): {lib().se2gpu_create_error().decode()}")
+        self._h = h
+        self.time = 0.0
+        self.step = 0
+        self._times = []
+
+    def _check(self, rc: int, what: str) -> int:
+        if rc < 0:
+            raise GpuError(f"{what} failed ({rc}): {lib().se2gpu_last_error(self._h).decode()}")
+        return rc
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().se2gpu_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_ptr: int):
+        self._check(lib().se2gpu_set_stream(self._h, C.c_void_p(stream_ptr)), "se2gpu_set_stream")
+
+    def synchronize(self):
+        self._check(lib().se2gpu_synchronize(self._h), "se2gpu_synchronize")
+
+    def advance(self, nsteps: int, stf: Optional[np.ndarray] = None):
+        """Advance nsteps (the host evaluates the STFs unless `stf` is given)."""
+        if nsteps <= 0:
+            return
+        times, stf_auto, t_end = self.setup.stf_block(self.time, nsteps)
+        if stf is None:
+            stf = stf_auto
+        stf = np.ascontiguousarray(stf, dtype=np.float64).reshape(-1)
+        self._check(lib().se2gpu_advance(self._h, nsteps, _p(stf) if stf.size else None), "se2gpu_advance")
+        if self.setup.nrec:
+            self._times.extend(times.tolist())
+        self.time = t_end
+        self.step += nsteps
+
+    def run(self, nsteps: Optional[int] = None, block: int = 1000) -> np.ndarray:
+        """Advance to the end of the reference's loop (or nsteps) and return the traces."""
+        n = self.setup.nsteps - self.step if nsteps is None else nsteps
+        rows = []
+        while n > 0:
+            k = min(n, block, self.trace_capacity) if self.setup.nrec else min(n, block)
+            self.advance(k)
+            n -= k
+            if self.setup.nrec:
+                rows.append(self.traces())
+        if not rows:
+            return np.zeros((0, 1 + 7 * self.setup.nrec))
+        return np.concatenate(rows, axis=0)
+
+    def traces(self) -> np.ndarray:
+        """Buffered receiver rows [time, (ux uy vx vy ax ay curl) per receiver], oldest first."""
+        nrec = self.setup.nrec
+        cap = max(self.trace_capacity, 1)
+        out = np.zeros((cap, 7 * max(nrec, 1)))
+        n = self._check(lib().se2gpu_traces(self._h, _p(out), cap), "se2gpu_traces")
+        times = np.array(self._times[:n])
+        del self._times[:n]
+        return np.concatenate([times.reshape(-1, 1), out[:n, : 7 * nrec]], axis=1)
+
+    def fields(self):
+        n = self.setup.ndof
+        u, v, a = np.zeros(n), np.zeros(n), np.zeros(n)
+        self._check(lib().se2gpu_get_fields(self._h, _p(u), _p(v), _p(a)), "se2gpu_get_fields")
+        return u, v, a
+
+    def set_fields(self, u=None, v=None, a=None):
+        arrs = [None if x is None else np.ascontiguousarray(x, dtype=np.float64) for x in (u, v, a)]
+        self._check(lib().se2gpu_set_fields(self._h, *[_p(x) for x in arrs]), "se2gpu_set_fields")
+
+    def norms(self) -> np.ndarray:
+        out = np.zeros(6)
+        self._check(lib().se2gpu_norms(self._h, _p(out)), "se2gpu_norms")
+        return out
+
+    def assemble_linear_form(self, u: np.ndarray) -> np.ndarray:
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        F = np.zeros(self.setup.ndof)
+        self._check(lib().se2gpu_assemble_linear_form(self._h, _p(u), _p(F)), "se2gpu_assemble_linear_form")
+        return F
+
+    def assemble_linear_form_device(self, u_ptr: int, F_ptr: int):
+        self._check(lib().se2gpu_assemble_linear_form_device(self._h, C.c_void_p(u_ptr), C.c_void_p(F_ptr)),
+                    "se2gpu_assemble_linear_form_device")
+
+    def info(self) -> dict:
+        a = (C.c_long * 8)()
+        self._check(lib().se2gpu_info(self._h, a), "se2gpu_info")
+        keys = ["nx_g", "ny_g", "p", "precision", "nsrc", "nrec", "launches", "rows"]
+        return dict(zip(keys, list(a)))
+
+    def device_fields(self):
+        u, v, a = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        self._check(lib().se2gpu_device_fields(self._h, C.byref(u), C.byref(v), C.byref(a)), "se2gpu_device_fields")
+        return u.value, v.value, a.value

@@ -1,0 +1,234 @@
+"""Parity of the sm_103a library with the reference (golden vectors made by the
+reference itself) and with the oracle port, through the C-ABI.
+
+FP64 mode must be bit-identical (np.array_equal) to the reference; FP32 with
+Kahan-compensated updates must stay within 1e-5 relative L2 of the FP64
+receiver traces (the tolerance the target states for FP32).
+"""
+import numpy as np
+import pytest
+
+from golden_util import load, spec_of
+from oracle import oracle as O
+from se2dr_fork_gb300 import gpu as G
+from se2dr_fork_gb300 import host as H
+from se2dr_fork_gb300 import spec as S
+
+pytestmark = pytest.mark.gpu
+
+FP32_TOL = 1e-5
+
+
+def rel_l2(x, ref):
+    den = np.linalg.norm(ref)
+    return np.linalg.norm(x - ref) / (den if den > 0 else 1.0)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib(gpu_lib):
+    return gpu_lib
+
+
+# ---------------------------------------------------------------- golden (the reference itself)
+@pytest.mark.parametrize("p", range(1, 9))
+def test_fp64_heterogeneous_traces_bitwise_vs_reference(p):
+    d = load(f"hetero_p{p}")
+    sol = G.Solver(H.Setup(spec_of(d)), "fp64")
+    tr = sol.run()
+    assert tr.shape == d["traces"].shape
+    assert np.array_equal(tr, d["traces"])
+    if "u" in d:
+        u, v, a = sol.fields()
+        assert np.array_equal(u, d["u"]) and np.array_equal(v, d["v"]) and np.array_equal(a, d["a"])
+
+
+@pytest.mark.parametrize("name", ["ragged_p4", "demo8_p2"])
+def test_fp64_fields_bitwise_vs_reference(name):
+    d = load(name)
+    sol = G.Solver(H.Setup(spec_of(d)), "fp64")
+    tr = sol.run()
+    assert np.array_equal(tr, d["traces"])
+    u, v, a = sol.fields()
+    assert np.array_equal(u, d["u"]) and np.array_equal(v, d["v"]) and np.array_equal(a, d["a"])
+
+
+@pytest.mark.parametrize("p", [1, 3, 4, 7])
+def test_fp64_internal_force_bitwise_vs_reference(p):
+    d = load(f"force_p{p}")
+    sol = G.Solver(H.Setup(spec_of(d)), "fp64")
+    F = sol.assemble_linear_form(d["u"])
+    assert np.array_equal(F, d["force"])
+
+
+def test_fp64_explosion64_full_run_bitwise_vs_reference():
+    d = load("explosion64")
+    sol = G.Solver(H.Setup(spec_of(d)), "fp64")
+    tr = sol.run()
+    assert tr.shape == d["traces"].shape == (4524, 8)
+    assert np.array_equal(tr, d["traces"])
+
+
+def test_fp32_kahan_explosion64_within_tolerance_of_reference():
+    d = load("explosion64")
+    sol = G.Solver(H.Setup(spec_of(d)), "fp32_kahan")
+    tr = sol.run()
+    ref = d["traces"]
+    assert np.array_equal(tr[:, 0], ref[:, 0])
+    errs = [rel_l2(tr[:, c], ref[:, c]) for c in range(1, 8)]
+    assert max(errs) <= FP32_TOL, errs
+
+
+def test_readme_demo_figure_features():
+    """Receiver-0 vy of the README run (docs/figs/se2wave-demo-vy.png) from the GPU."""
+    d = load("readme_demo64")
+    sol = G.Solver(H.Setup(S.demo(64, p=6)), "fp64")
+    tr = sol.run()
+    assert np.array_equal(tr[:, 0], d["time"]) and np.array_equal(tr[:, 4], d["vy0"])
+    t, vy = tr[:, 0], tr[:, 4]
+    pk = (t > 0.145) & (t < 0.175)
+    tr_ = (t > 0.175) & (t < 0.2)
+    assert abs(vy[pk].max() - 5.2e-9) < 0.2e-9 and abs(t[pk][vy[pk].argmax()] - 0.16) < 0.005
+    assert abs(vy[tr_].min() + 6.0e-9) < 0.2e-9 and abs(t[tr_][vy[tr_].argmin()] - 0.187) < 0.005
+
+
+# ---------------------------------------------------------------- oracle port, other shapes
+@pytest.mark.parametrize("p,mx,my", [(1, 40, 3), (2, 17, 33), (3, 12, 23), (4, 9, 17), (5, 7, 13),
+                                     (6, 11, 6), (7, 5, 9), (8, 9, 5), (4, 1, 1), (6, 1, 7)])
+def test_fp64_vs_oracle_ragged_meshes(p, mx, my):
+    rng = np.random.default_rng(p * 100 + mx)
+    Lx = 2000.0
+    sp = S.explosion64(mx, my, p=p, tmax=1.0).replace(
+        nt=25, nearest_internal_gll=(p > 1),
+        cell_vp=rng.uniform(5000, 7000, mx * my), cell_vs=rng.uniform(2800, 3500, mx * my),
+        cell_rho=rng.uniform(2000, 3000, mx * my),
+        sources=[S.Source(rng.uniform(-1000, 1000), rng.uniform(-1000, 1000), tuple(rng.normal(0, 1e15, 4)),
+                          S.STF_RICKER, (0.002, 60.0, 1.0)) for _ in range(3)],
+        receivers=[tuple(rng.uniform(-Lx / 2, Lx / 2, 2)) for _ in range(4)] + [(-1000.0, -1000.0), (1000.0, 1000.0)])
+    sol = G.Solver(H.Setup(sp), "fp64")
+    tr = sol.run()
+    ref = O.OracleSolver(sp)
+    rr = ref.run(10 ** 6)
+    assert np.array_equal(tr, rr["traces"])
+    u, v, a = sol.fields()
+    ru, rv, ra = ref.state()
+    assert np.array_equal(u, ru) and np.array_equal(v, rv) and np.array_equal(a, ra)
+
+
+def test_fp64_norms_vs_oracle():
+    sp = S.demo(10, 7, p=4, tmax=1.0).replace(nt=200)
+    sol = G.Solver(H.Setup(sp), "fp64")
+    sol.run()
+    ref = O.OracleSolver(sp)
+    rr = ref.run(10 ** 6, norms=True)
+    last = rr["norms"][-1, 1:]
+    np.testing.assert_allclose(sol.norms(), last, rtol=1e-12, atol=0)
+
+
+def test_fp64_set_fields_then_step_matches_oracle():
+    sp = S.demo(6, 6, p=5, tmax=1.0).replace(nt=10)
+    setup = H.Setup(sp)
+    rng = np.random.default_rng(5)
+    u0, v0, a0 = (rng.standard_normal(setup.ndof) * s for s in (1e-6, 1e-3, 1.0))
+    sol = G.Solver(setup, "fp64")
+    sol.set_fields(u0, v0, a0)
+    tr = sol.run()
+    ref = O.OracleSolver(sp)
+    ref.set_state(u0, v0, a0)
+    rr = ref.run(10 ** 6)
+    assert np.array_equal(tr, rr["traces"])
+    assert all(np.array_equal(x, y) for x, y in zip(sol.fields(), ref.state()))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32_kahan", "fp32"])
+def test_deterministic_repeat(precision):
+    d = load("hetero_p4")
+    runs = []
+    for _ in range(2):
+        sol = G.Solver(H.Setup(spec_of(d)), precision)
+        runs.append((sol.run(), *sol.fields()))
+    assert all(np.array_equal(x, y) for x, y in zip(*runs))
+
+
+@pytest.mark.parametrize("p", [2, 4, 6, 8])
+def test_fp32_kahan_vs_fp64(p):
+    sp = S.explosion64(16, 16, p=p, tmax=0.25)
+    setup = H.Setup(sp)
+    t64 = G.Solver(setup, "fp64").run()
+    t32 = G.Solver(setup, "fp32_kahan").run()
+    errs = [rel_l2(t32[:, c], t64[:, c]) for c in range(1, 8)]
+    assert max(errs) <= FP32_TOL, errs
+
+
+def test_internal_force_device_entry_point():
+    import torch
+    d = load("force_p4")
+    sol = G.Solver(H.Setup(spec_of(d)), "fp64")
+    u = torch.tensor(d["u"], dtype=torch.float64, device="cuda")
+    F = torch.empty_like(u)
+    sol.set_stream(torch.cuda.current_stream().cuda_stream)
+    sol.assemble_linear_form_device(u.data_ptr(), F.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(F.cpu().numpy(), d["force"])
+
+
+# ---------------------------------------------------------------- full-size properties (2048^2, degree 4)
+# 67M nodes: too large for the CPU oracle, so these check size-independent
+# properties with every tile active (random initial fields).
+@pytest.fixture(scope="module")
+def grf_setup():
+    return H.Setup(S.grf2048(nt=24))
+
+
+@pytest.fixture(scope="module")
+def grf_u0(grf_setup):
+    rng = np.random.default_rng(2048)
+    return rng.standard_normal(grf_setup.ndof) * 1e-3
+
+
+def _full_run(setup, precision, u0, scale, nsteps=24):
+    sol = G.Solver(setup, precision)
+    sol.set_fields(u=scale * u0)
+    t = 0.0
+    times, stf, t = setup.stf_block(t, nsteps)
+    sol.advance(nsteps, stf=scale * stf)
+    tr = sol.traces()
+    u, v, a = sol.fields()
+    sol.close()
+    return tr, u, v, a
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32_kahan"])
+def test_full_size_linearity(grf_setup, grf_u0, precision):
+    """Doubling the initial field and the moment doubles every field exactly
+    (scaling by 2 commutes with every rounding)."""
+    r1 = _full_run(grf_setup, precision, grf_u0, 1.0)
+    r2 = _full_run(grf_setup, precision, grf_u0, 2.0)
+    for x1, x2 in zip(r1, r2):
+        assert np.array_equal(x2[..., 1:] if x2.ndim == 2 else x2, 2.0 * (x1[..., 1:] if x1.ndim == 2 else x1))
+
+
+def test_full_size_fp32_kahan_vs_fp64(grf_setup, grf_u0):
+    r64 = _full_run(grf_setup, "fp64", grf_u0, 1.0)
+    r32 = _full_run(grf_setup, "fp32_kahan", grf_u0, 1.0)
+    for x32, x64 in zip(r32[1:], r64[1:]):
+        assert rel_l2(x32, x64) <= FP32_TOL
+    assert rel_l2(r32[0][:, 1:], r64[0][:, 1:]) <= FP32_TOL
+
+
+def test_full_size_deterministic(grf_setup, grf_u0):
+    r1 = _full_run(grf_setup, "fp32_kahan", grf_u0, 1.0, nsteps=8)
+    r2 = _full_run(grf_setup, "fp32_kahan", grf_u0, 1.0, nsteps=8)
+    assert all(np.array_equal(x, y) for x, y in zip(r1, r2))
+
+
+# ---------------------------------------------------------------- errors are reported, not crashed
+def test_errors_are_reported():
+    sp = S.demo(4, 4, p=2, tmax=1.0).replace(nt=8)
+    setup = H.Setup(sp)
+    with pytest.raises(G.GpuError):
+        G.Solver(setup, 17)
+    sol = G.Solver(setup, "fp64", trace_capacity=4)
+    with pytest.raises(G.GpuError):
+        sol.advance(5)
+    sol.advance(4)
+    assert sol.traces().shape == (4, 22)

@@ -1,0 +1,121 @@
+"""The product's FP64 host set-up (libse2host.so) against the reference's golden
+vectors and the oracle port, plus its input checks and the material generator."""
+import platform
+
+import numpy as np
+import pytest
+
+from golden_util import load, spec_of
+from oracle import oracle as O
+from se2dr_fork_gb300 import host as H
+from se2dr_fork_gb300 import spec as S
+
+BITWISE = platform.machine() in ("x86_64", "AMD64")
+
+
+def same(x, ref, tol=1e-12):
+    if BITWISE:
+        return np.array_equal(x, ref)
+    den = np.linalg.norm(ref)
+    return np.linalg.norm(np.asarray(x) - ref) <= tol * (den if den > 0 else 1.0)
+
+
+@pytest.mark.parametrize("p", range(1, 9))
+def test_setup_vs_reference(p):
+    d = load(f"hetero_p{p}")
+    s = H.Setup(spec_of(d))
+    assert same(s.D.ravel(), d["D"]) and same(s.xi, d["xi"]) and same(s.w1d, d["w1d"])
+    assert same(s.src_vals.ravel(), d["src_values"])
+    assert np.array_equal(np.stack([s.src_elem, s.src_gll], 1).ravel(), d["src_index"])
+    assert same(np.array([s.dt_cfl]), d["dt_cfl"])
+    assert s.nsteps == d["traces"].shape[0]
+    if "mass" in d:
+        assert same(s.mass_vec(), d["mass"]) and same(s.coords(), d["coords"])
+
+
+@pytest.mark.parametrize("p", [1, 3, 6, 8])
+def test_setup_vs_oracle_bitwise(p):
+    """Same host, same libm: the product set-up and the oracle agree bit for bit."""
+    rng = np.random.default_rng(p)
+    mx, my = 9, 4
+    sp = S.explosion64(mx, my, p=p).replace(
+        nearest_internal_gll=(p > 1), cell_vp=rng.uniform(4000, 6000, mx * my),
+        cell_vs=rng.uniform(2000, 3000, mx * my), cell_rho=rng.uniform(2000, 3000, mx * my),
+        receivers=[(500.0, 500.0), (-1000.0, 999.99), (3.3, -444.4)])
+    s, o = H.Setup(sp), O.OracleSolver(sp)
+    assert np.array_equal(s.mass_vec(), o.get("mass"))
+    assert np.array_equal(s.coords(), o.get("coords"))
+    assert np.array_equal(s.D.ravel(), o.get("D"))
+    assert s.dt == o.dt and s.nsteps == o.nsteps_planned
+    assert np.array_equal(np.stack([s.rec_node, s.rec_elem, s.rec_gll], 1).ravel(), o.get("rec_index"))
+    assert np.array_equal(s.src_vals.ravel(), o.get("src_values"))
+
+
+def test_gll_closed_form():
+    """GLL nodes are the roots of (1-x^2) P'_N and weights 2/(N(N+1) P_N(x)^2)."""
+    from numpy.polynomial import legendre as L
+    for p in range(1, 9):
+        xi, w = H.gll(p)
+        c = np.zeros(p + 1); c[-1] = 1
+        interior = np.sort(L.legroots(L.legder(c)))
+        np.testing.assert_allclose(xi, np.concatenate([[-1.0], interior, [1.0]]), atol=1e-14)
+        np.testing.assert_allclose(np.sort(w), np.sort(2.0 / (p * (p + 1) * L.legval(xi, c) ** 2)), rtol=1e-13)
+        assert abs(w.sum() - 2.0) < 1e-14
+
+
+def test_derivative_matrix_closed_form():
+    """D_ij = P_N(x_i) / (P_N(x_j) (x_i - x_j)), D_00 = -N(N+1)/4, D_NN = +N(N+1)/4, else 0."""
+    from numpy.polynomial import legendre as L
+    for p in range(1, 9):
+        s = H.Setup(S.demo(2, p=max(p, 2)).replace(p=p, nearest_internal_gll=False, sources=[], receivers=[]))
+        x = s.xi
+        c = np.zeros(p + 1); c[-1] = 1
+        PN = L.legval(x, c)
+        Dc = np.zeros((p + 1, p + 1))
+        for i in range(p + 1):
+            for j in range(p + 1):
+                if i != j:
+                    Dc[i, j] = PN[i] / (PN[j] * (x[i] - x[j]))
+        Dc[0, 0] = -p * (p + 1) / 4.0
+        Dc[p, p] = p * (p + 1) / 4.0
+        np.testing.assert_allclose(s.D, Dc, atol=1e-11 * max(1.0, np.abs(Dc).max()))
+
+
+def test_stf_vs_reference():
+    g = load("stf")
+    t = g["ricker"][:, 0]
+    vals = np.array([H.stf_eval(0, (0.15, 12.0, 1.0), x) for x in t])
+    assert same(vals, g["ricker"][:, 1])
+    t = g["yoffe_mode2"][:, 0]
+    vals = np.array([H.stf_eval(2, (0.3, 0.45, 1.1), x) for x in t])
+    assert same(vals, g["yoffe_mode2"][:, 1])
+
+
+def test_setup_rejects_bad_input():
+    bad = [S.demo(4).replace(sources=[S.Source(5000.0, 0.0, (1, 0, 0, 1))]),       # source outside
+           S.demo(4, p=1),                                                        # p=1, interior GLL rule
+           S.demo(4).replace(receivers=[(0.0, 1e6)]),                             # receiver outside
+           S.demo(4).replace(p=9),                                                # degree beyond 8
+           S.demo(4).replace(sources=[S.Source(0, 0, (1, 0, 0, 1), S.STF_YOFFE, (0.2, 0.2, 1.0))]),  # bad Yoffe
+           S.demo(4).replace(rho=-1.0)]
+    for sp in bad:
+        with pytest.raises(ValueError):
+            H.Setup(sp)
+
+
+def test_gaussian_random_field_statistics():
+    vp = H.gaussian_random_field(256, 256, 5000.0, 0.1, 8.0, seed=1)
+    assert abs(vp.mean() - 5000.0) < 100.0
+    assert 350.0 < vp.std() < 650.0
+    assert vp.min() >= 5000.0 * 0.7 - 1e-9 and vp.max() <= 5000.0 * 1.3 + 1e-9
+    z = (vp.reshape(256, 256) - vp.mean()) / vp.std()
+    r1 = (z[:, :-1] * z[:, 1:]).mean()      # neighbour correlation of a Gaussian kernel, std 8 cells
+    r16 = (z[:, :-16] * z[:, 16:]).mean()
+    assert r1 > 0.95 and r16 < 0.5
+    assert np.array_equal(vp, H.gaussian_random_field(256, 256, 5000.0, 0.1, 8.0, seed=1))
+
+
+def test_nsteps_matches_reference_loop():
+    d = load("explosion64")
+    s = H.Setup(spec_of(d))
+    assert s.nsteps == 4524 == d["traces"].shape[0]
