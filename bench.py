@@ -48,8 +48,8 @@ def alg_bytes_per_node(precision: str, ne: int, nnodes: int) -> float:
     if precision == "fp64":
         return 2 * 3 * 16 + 8 + 16 * cell          # u,v,a (double2) in+out, M, (lambda, mu)
     if precision == "fp32_kahan":
-        return 2 * 5 * 8 + 4 + 8 * cell            # u,v,a,cu,cv (float2) in+out, 1/M, (lambda, mu)
-    return 2 * 3 * 8 + 4 + 8 * cell
+        return 2 * 4 * 8 + 4 + 8 * cell            # leapfrog u,w,cu,cw (float2) in+out, 1/M, (lambda, mu)
+    return 2 * 2 * 8 + 4 + 8 * cell                # leapfrog u,w (float2) in+out, 1/M, (lambda, mu)
 
 
 class ClockSampler:
@@ -193,19 +193,29 @@ def run_ours(args, rank, world):
     stream = torch.cuda.Stream()
     hbm, peak_kind = peaks()
     results = {}
+    from se2dr_fork_gb300 import autotune
+    tuned = None
+    if args.autotune and args.precision != "fp64":
+        tuned = autotune.tune(setup, args.precision, steps=10)
     for prec in [args.precision] + (["fp64"] if args.precision != "fp64" and not args.no_fp64 else []):
         k = args.steps if prec == args.precision else max(3, args.steps // 8)
         sol = G.Solver(setup, prec, trace_capacity=k + args.warmup + 2)
+        if prec != "fp64":
+            if args.tile_config >= 0:
+                sol.set_tile_config(args.tile_config)
+            else:
+                autotune.apply(sol, prec)
         sol.set_stream(stream.cuda_stream)
         barrier()
         with ClockSampler(local) as clk:
             secs, launches = time_steps(sol, k, args.warmup, stream, torch)
         secs = tmax(secs)
+        tile = sol.tile_configs()[sol.tile_config] if prec != "fp64" else None
         sol.close()
         per = secs / k
         b = alg_bytes_per_node(prec, ne, nnodes)
         achieved = b * nnodes / per / 1e9
-        results[prec] = {"value": world * dof * k / secs, "ms_per_step": 1e3 * per, "steps": k,
+        results[prec] = {"value": world * dof * k / secs, "ms_per_step": 1e3 * per, "steps": k, "tile": tile,
                          "launches": launches, "clocks": clk.summary(),
                          "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                                       "frac": achieved / hbm, "traffic": None,
@@ -216,6 +226,11 @@ def run_ours(args, rank, world):
     barrier()
     t0 = time.perf_counter()
     sol = G.Solver(setup, prec, trace_capacity=args.steps + 2)
+    if prec != "fp64":
+        if args.tile_config >= 0:
+            sol.set_tile_config(args.tile_config)
+        else:
+            autotune.apply(sol, prec)
     sol.advance(args.steps)
     tr = sol.traces()
     sol.close()
@@ -248,9 +263,10 @@ def run_ours(args, rank, world):
                                    f"Gaussian-random-field Vp (mean 5000, 10% std, corr 8 cells), Vp/Vs 1.73, "
                                    f"rho 2700, explosive Ricker f0 8 Hz, 64 receivers",
                        "precision": prec, "nodes": nnodes, "dof": dof, "parallelism": f"replicas x{world}",
-                       "l2": "inputs larger than L2 (state %.1f GB)" % ((10 if prec == "fp32_kahan" else 6)
+                       "l2": "inputs larger than L2 (state %.1f GB)" % ({"fp32_kahan": 8, "fp32": 4, "fp64": 6}[prec]
                                                                        * nnodes * (4 if prec != 'fp64' else 8) * 2 / 1e9)},
             "roofline": head["roofline"], "clocks": head["clocks"], "gpu_launches": head["launches"],
+            "tile": head.get("tile"), "autotune": tuned,
             "e2e": {"value": world * dof * args.steps / e2e_s, "unit": "DOF/s", "h2d_bytes_per_step": h2d / args.steps,
                     "d2h_bytes_per_step": d2h / args.steps, "seconds": e2e_s,
                     "includes": "se2gpu_create (upload of the set-up from host memory), advance, traces, destroy"},
@@ -276,6 +292,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-rows", type=int, default=32)
     ap.add_argument("--cpu-steps", type=int, default=6)
+    ap.add_argument("--tile-config", type=int, default=-1, help="step-kernel tile configuration (-1: autotuned or default)")
+    ap.add_argument("--autotune", action="store_true", help="measure every tile configuration first and cache the best")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

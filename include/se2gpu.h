@@ -50,6 +50,7 @@ typedef struct se2gpu_problem {
   double dt;                 /* time step */
   const double *D;           /* (p+1)^2: D[q*(p+1)+i] = dN_i/dxi at GLL point q */
   const double *wq;          /* (p+1)^2: tensor GLL weights w[i+j*(p+1)] */
+  const double *w1d;         /* p+1: 1-D GLL weights (wq[i+j*(p+1)] = w1d[i]*w1d[j]) */
   const double *J00, *J11;   /* mx, my: element half-widths */
   const double *iJ00, *iJ11; /* mx, my: their reciprocals */
   const double *lambda, *mu; /* mx*my cell Lame parameters */
@@ -103,10 +104,21 @@ int se2gpu_assemble_linear_form(se2gpu_solver *h, const double *u, double *F);
    launched on the handle's stream, no synchronisation. */
 int se2gpu_assemble_linear_form_device(se2gpu_solver *h, const void *u_dev, void *F_dev);
 
-/* Introspection: ints[0..7] = nx_g, ny_g, p, precision, nsrc, nrec, kernel
-   launches so far, buffered trace rows; device pointers of the current u, v, a. */
+/* Introspection: ints[0..8] = nx_g, ny_g, p, precision, nsrc, nrec, kernel
+   launches so far, buffered trace rows, device row pitch (nodes). */
 int se2gpu_info(const se2gpu_solver *h, long *ints);
+
+/* Device pointers of the current state.  FP64: u, v, a in the reference's
+   packed layout.  FP32 modes hold the leapfrog state in rows of `pitch` nodes
+   (float2 per node): u = displacement of the next step, v = half-step velocity
+   (v_k + dt/2 a_k), a = acceleration of the last step. */
 int se2gpu_device_fields(const se2gpu_solver *h, void **u, void **v, void **a);
+
+/* Tile configurations of the step kernel (elements per tile edge, threads per
+   CTA) available for the handle's degree and precision, for the autotuner;
+   returns how many exist.  se2gpu_set_tile_config selects one (default 0). */
+int se2gpu_tile_configs(const se2gpu_solver *h, int *edge, int *threads, int max_configs);
+int se2gpu_set_tile_config(se2gpu_solver *h, int config);
 
 #ifdef __cplusplus
 }

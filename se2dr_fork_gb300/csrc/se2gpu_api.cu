@@ -1,10 +1,14 @@
 // se2gpu_api.cu -- C-ABI of libse2gpu.so (see include/se2gpu.h).
 //
-// Owns the device memory of one problem: two buffer sets of the fields (the
-// step kernel reads one and writes the other), the per-cell and per-axis
-// tables, sources, receivers and the device trace buffer.  Every entry point
-// validates its arguments on the host and returns a status code; CUDA errors
-// are caught after each launch and reported through se2gpu_last_error.
+// FP64 mode keeps the reference's state (u, v, a) in the reference's packed
+// [node][component] layout and runs the tiled reference-order kernel
+// (se2gpu_kernels.cuh).  FP32 modes keep the leapfrog state (u, w = half-step
+// velocity, Kahan terms) in a padded layout (row pitch a multiple of 16 nodes,
+// as the TMA copies require) and run the persistent TMA-pipelined kernel
+// (se2gpu_persist.cuh); set/get_fields convert to and from the reference's
+// (u, v, a) in FP64 on the host.  Every entry point validates its arguments on
+// the host and returns a status code; CUDA errors and the kernels' bounded-wait
+// error flag are reported through se2gpu_last_error.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -12,10 +16,12 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <vector>
 
 #include "se2gpu.h"
 #include "se2gpu_launch.h"
+#include "se2gpu_persist_launch.h"
 
 struct se2gpu_solver {
   int mx, my, p, n1, npe, nx_g, ny_g, precision;
@@ -23,18 +29,30 @@ struct se2gpu_solver {
   int nsrc, nrec, trace_cap, rows_written;
   bool pending_record;
   double dt;
-  int device;
+  int device, nsm;
   cudaStream_t stream, own_stream;
-  size_t tsize;                  // bytes per scalar (4 or 8)
-  void *fields[2][5];            // [buffer][u v a cu cv]
+  size_t tsize;                  // compute precision (4 or 8 bytes)
+  // FP64 state: two buffer sets of packed u, v, a
+  void *f64[2][3];
   int cur;
+  // FP32 leapfrog state (padded): u, w, cu, cw per buffer set, a of the last step
+  int pitch;
+  float2 *pu[2], *pw[2], *pcu[2], *pcw[2], *pa;
+  float *pminv, *rbuf[2];
+  int rlast;
+  CUtensorMap maps[2][4];
+  int pgrid, pconfig, pntx, pnty;
+  int *tile_src_off, *tile_src_idx, *tile_rec_off, *tile_rec_idx;
+  std::vector<int> *src_elem_h, *rec_elem_h;
+  int *err_dev;
+  // tables in compute precision
   void *mass, *lam, *mu, *J00, *J11, *iJ00, *iJ11, *D, *wq, *src_vals;
   double *Dd, *iJ00d, *iJ11d, *stf_dev, *traces, *norm_part;
   int stf_cap;
   int *src_elem, *rec_node, *rec_elem, *rec_gll;
-  void *scratch_u, *scratch_f;   // assemble_linear_form staging
+  void *scratch_u, *scratch_f;   // assemble_linear_form staging (packed)
   long launches;
-  int ntx, nty, nblocks;
+  int ntx, nty, nblocks;         // FP64 tiles
   char err[512];
 };
 
@@ -53,12 +71,15 @@ static int fail(se2gpu_solver *h, int code, const char *fmt, ...)
   return code;
 }
 
-#define CK(h, call)                                                                                     \
-  do {                                                                                                  \
-    cudaError_t e_ = (call);                                                                            \
-    if (e_ != cudaSuccess) return fail((h), SE2GPU_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
-                                       __FILE__, __LINE__);                                             \
+#define CK(h, call)                                                                                              \
+  do {                                                                                                           \
+    cudaError_t e_ = (call);                                                                                     \
+    if (e_ != cudaSuccess) return fail((h), SE2GPU_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_),    \
+                                       __FILE__, __LINE__);                                                      \
   } while (0)
+
+static bool is_f64(const se2gpu_solver *h) { return h->precision == SE2GPU_FP64; }
+static bool is_kahan(const se2gpu_solver *h) { return h->precision == SE2GPU_FP32_KAHAN; }
 
 static int dalloc(se2gpu_solver *h, void **p, size_t bytes)
 {
@@ -69,6 +90,14 @@ static int dalloc(se2gpu_solver *h, void **p, size_t bytes)
     cudaGetLastError();
     return fail(h, SE2GPU_ERR_NOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
   }
+  return 0;
+}
+
+static int dzero(se2gpu_solver *h, void **p, size_t bytes)
+{
+  int rc = dalloc(h, p, bytes);
+  if (rc) return rc;
+  CK(h, cudaMemset(*p, 0, bytes ? bytes : 16));
   return 0;
 }
 
@@ -108,14 +137,108 @@ extern "C" void se2gpu_destroy(se2gpu_solver *h)
   if (!h) return;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
-  for (int b = 0; b < 2; b++)
-    for (int f = 0; f < 5; f++) cudaFree(h->fields[b][f]);
-  void *ptrs[] = {h->mass, h->lam, h->mu, h->J00, h->J11, h->iJ00, h->iJ11, h->D, h->wq, h->src_vals,
-                  h->Dd, h->iJ00d, h->iJ11d, h->stf_dev, h->traces, h->norm_part, h->src_elem, h->rec_node,
-                  h->rec_elem, h->rec_gll, h->scratch_u, h->scratch_f};
+  for (int b = 0; b < 2; b++) {
+    for (int f = 0; f < 3; f++) cudaFree(h->f64[b][f]);
+    cudaFree(h->pu[b]); cudaFree(h->pw[b]); cudaFree(h->pcu[b]); cudaFree(h->pcw[b]); cudaFree(h->rbuf[b]);
+  }
+  void *ptrs[] = {h->pa, h->pminv, h->err_dev, h->mass, h->lam, h->mu, h->J00, h->J11, h->iJ00, h->iJ11, h->D, h->wq,
+                  h->src_vals, h->Dd, h->iJ00d, h->iJ11d, h->stf_dev, h->traces, h->norm_part, h->src_elem,
+                  h->rec_node, h->rec_elem, h->rec_gll, h->scratch_u, h->scratch_f, h->tile_src_off,
+                  h->tile_src_idx, h->tile_rec_off, h->tile_rec_idx};
   for (void *p : ptrs) cudaFree(p);
+  delete h->src_elem_h;
+  delete h->rec_elem_h;
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   free(h);
+}
+
+// the FP32 leapfrog state of the reference's (u, v, a) at step k:
+// w = v + dt/2 a, u' = u + dt w, stored as FP32 value + Kahan residual (true = hi - lo)
+static int upload_leapfrog(se2gpu_solver *h, const double *u, const double *v, const double *a)
+{
+  const size_t np = (size_t)h->ny_g * h->pitch;
+  std::vector<float2> U(np), W(np), CU(np), CW(np), A(np);
+  const double dt = h->dt, hdt = 0.5 * h->dt;
+  for (long y = 0; y < h->ny_g; y++)
+    for (long x = 0; x < h->nx_g; x++) {
+      const size_t n = (size_t)(y * h->nx_g + x), k = (size_t)(y * h->pitch + x);
+      double wv[2], uv[2];
+      for (int c = 0; c < 2; c++) {
+        const double uu = u ? u[2 * n + c] : 0.0, vv = v ? v[2 * n + c] : 0.0, aa = a ? a[2 * n + c] : 0.0;
+        wv[c] = vv + hdt * aa;
+        uv[c] = uu + dt * wv[c];
+      }
+      W[k] = make_float2((float)wv[0], (float)wv[1]);
+      U[k] = make_float2((float)uv[0], (float)uv[1]);
+      CW[k] = make_float2((float)((double)W[k].x - wv[0]), (float)((double)W[k].y - wv[1]));
+      CU[k] = make_float2((float)((double)U[k].x - uv[0]), (float)((double)U[k].y - uv[1]));
+      A[k] = make_float2(a ? (float)a[2 * n] : 0.f, a ? (float)a[2 * n + 1] : 0.f);
+    }
+  const int c = h->cur;
+  CK(h, cudaMemcpy(h->pu[c], U.data(), np * 8, cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpy(h->pw[c], W.data(), np * 8, cudaMemcpyHostToDevice));
+  if (is_kahan(h)) {
+    CK(h, cudaMemcpy(h->pcu[c], CU.data(), np * 8, cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(h->pcw[c], CW.data(), np * 8, cudaMemcpyHostToDevice));
+  }
+  CK(h, cudaMemcpy(h->pa, A.data(), np * 8, cudaMemcpyHostToDevice));
+  return 0;
+}
+
+// select one of the persistent kernel's tile configurations: kernel attributes,
+// tensor-map boxes, per-tile source/receiver lists and the persistent grid
+static int setup_f32_config(se2gpu_solver *h, int config)
+{
+  const bool kahan = is_kahan(h);
+  se2p::TileShape ts;
+  if (se2p::config_shape(h->p, config, kahan, &ts)) return fail(h, SE2GPU_ERR_ARG, "no tile configuration %d for degree %d", config, h->p);
+  CK(h, cudaStreamSynchronize(h->stream));
+  {
+    cudaError_t e = se2p::prepare(h->p, config, kahan);
+    if (e != cudaSuccess) return fail(h, SE2GPU_ERR_CUDA, "persistent kernel set-up: %s", cudaGetErrorString(e));
+  }
+  for (int b = 0; b < 2; b++) {
+    void *bases[4] = {h->pu[b], kahan ? (void *)h->pcu[b] : (void *)h->pu[b], h->pw[b], kahan ? (void *)h->pcw[b] : (void *)h->pw[b]};
+    for (int m = 0; m < 4; m++) {
+      const int bw = (m < 2) ? ts.region_w : ts.own_w, bh = (m < 2) ? ts.region_h : ts.own_h;
+      const int r = se2p::make_map(&h->maps[b][m], bases[m], h->nx_g, h->ny_g, h->pitch, bw, bh);
+      if (r) return fail(h, SE2GPU_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", r);
+    }
+  }
+  const int te = ts.tex, P = h->p;
+  const int ntx = (h->mx + te - 1) / te, nty = (h->my + te - 1) / te, ntiles = ntx * nty;
+  // tile lists: a source or receiver element appears in every tile whose owned nodes it touches
+  auto build = [&](const std::vector<int> &elems, std::vector<int> &off, std::vector<int> &idx) {
+    std::vector<std::vector<int>> per(ntiles);
+    for (int q = 0; q < (int)elems.size(); q++) {
+      const int ex = elems[q] % h->mx, ey = elems[q] / h->mx;
+      for (int ty = std::max(0, (ey - 1) / te); ty <= std::min(nty - 1, (ey + 1) / te); ty++)
+        for (int tx = std::max(0, (ex - 1) / te); tx <= std::min(ntx - 1, (ex + 1) / te); tx++) {
+          const int X0 = tx * te * P, X1 = std::min((tx + 1) * te, h->mx) * P + (((tx + 1) * te >= h->mx) ? 1 : 0);
+          const int Y0 = ty * te * P, Y1 = std::min((ty + 1) * te, h->my) * P + (((ty + 1) * te >= h->my) ? 1 : 0);
+          if (ex * P <= X1 - 1 && ex * P + P >= X0 && ey * P <= Y1 - 1 && ey * P + P >= Y0) per[ty * ntx + tx].push_back(q);
+        }
+    }
+    off.assign(ntiles + 1, 0);
+    for (int t = 0; t < ntiles; t++) off[t + 1] = off[t] + (int)per[t].size();
+    idx.clear();
+    for (int t = 0; t < ntiles; t++) idx.insert(idx.end(), per[t].begin(), per[t].end());
+  };
+  std::vector<int> so, si, ro, ri;
+  build(*h->src_elem_h, so, si);
+  build(*h->rec_elem_h, ro, ri);
+  cudaFree(h->tile_src_off); cudaFree(h->tile_src_idx); cudaFree(h->tile_rec_off); cudaFree(h->tile_rec_idx);
+  h->tile_src_off = h->tile_src_idx = h->tile_rec_off = h->tile_rec_idx = nullptr;
+  int rc;
+  if ((rc = upload_i(h, &h->tile_src_off, so.data(), so.size()))) return rc;
+  if ((rc = upload_i(h, &h->tile_src_idx, si.data(), si.size()))) return rc;
+  if ((rc = upload_i(h, &h->tile_rec_off, ro.data(), ro.size()))) return rc;
+  if ((rc = upload_i(h, &h->tile_rec_idx, ri.data(), ri.size()))) return rc;
+  h->pconfig = config;
+  h->pntx = ntx;
+  h->pnty = nty;
+  h->pgrid = std::min(ntiles, std::max(1, se2p::occupancy(P, config, kahan)) * h->nsm);
+  return 0;
 }
 
 extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_capacity, se2gpu_solver **out)
@@ -131,7 +254,7 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
   if (nx_g * ny_g * 2 >= 2147483647L) return fail(nullptr, SE2GPU_ERR_ARG, "mesh too large for 32-bit node indices");
   if (!(P->dt > 0.0) || !std::isfinite(P->dt)) return fail(nullptr, SE2GPU_ERR_ARG, "time step must be positive and finite");
   if (P->nsrc < 0 || P->nrec < 0 || trace_capacity < 0) return fail(nullptr, SE2GPU_ERR_ARG, "negative count");
-  if (!P->D || !P->wq || !P->J00 || !P->J11 || !P->iJ00 || !P->iJ11 || !P->lambda || !P->mu || !P->mass)
+  if (!P->D || !P->wq || !P->w1d || !P->J00 || !P->J11 || !P->iJ00 || !P->iJ11 || !P->lambda || !P->mu || !P->mass)
     return fail(nullptr, SE2GPU_ERR_ARG, "missing problem table");
   if (P->nsrc && (!P->src_elem || !P->src_vals)) return fail(nullptr, SE2GPU_ERR_ARG, "missing source arrays");
   if (P->nrec && (!P->rec_node || !P->rec_elem || !P->rec_gll)) return fail(nullptr, SE2GPU_ERR_ARG, "missing receiver arrays");
@@ -161,29 +284,16 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
   int rc;
 #define TRY(x) do { if ((rc = (x)) != 0) { snprintf(g_create_err, sizeof(g_create_err), "%s", h->err); se2gpu_destroy(h); return rc; } } while (0)
   if (cudaGetDevice(&h->device) != cudaSuccess) { cudaGetLastError(); free(h); return fail(nullptr, SE2GPU_ERR_CUDA, "no CUDA device"); }
+  cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->device);
   {
     cudaError_t e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { free(h); return fail(nullptr, SE2GPU_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e)); }
     h->stream = h->own_stream;
   }
   {
-    cudaError_t e = (precision == SE2GPU_FP64) ? se2::prepare_f64(P->p) : se2::prepare_f32(P->p, precision == SE2GPU_FP32_KAHAN);
+    // the tiled kernels serve FP64 and the FP32 internal-force entry point
+    cudaError_t e = (precision == SE2GPU_FP64) ? se2::prepare_f64(P->p) : se2::prepare_f32(P->p, false);
     if (e != cudaSuccess) { fail(h, SE2GPU_ERR_CUDA, "kernel set-up: %s", cudaGetErrorString(e)); TRY(SE2GPU_ERR_CUDA); }
-  }
-  const size_t vbytes = (size_t)nnodes * 2 * h->tsize;
-  const int nf = (precision == SE2GPU_FP32_KAHAN) ? 5 : 3;
-  for (int b = 0; b < 2; b++)
-    for (int f = 0; f < nf; f++) {
-      TRY(dalloc(h, &h->fields[b][f], vbytes));
-      if (cudaMemset(h->fields[b][f], 0, vbytes) != cudaSuccess) { fail(h, SE2GPU_ERR_CUDA, "cudaMemset failed"); TRY(SE2GPU_ERR_CUDA); }
-    }
-  // mass: FP64 keeps M (the reference divides); FP32 stores 1/M computed in FP64
-  if (precision == SE2GPU_FP64) {
-    TRY(upload(h, &h->mass, P->mass, (size_t)nnodes));
-  } else {
-    std::vector<double> minv((size_t)nnodes);
-    for (long i = 0; i < nnodes; i++) minv[i] = 1.0 / P->mass[i];
-    TRY(upload(h, &h->mass, minv.data(), (size_t)nnodes));
   }
   TRY(upload(h, &h->lam, P->lambda, (size_t)ne));
   TRY(upload(h, &h->mu, P->mu, (size_t)ne));
@@ -203,6 +313,39 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
   TRY(upload_i(h, &h->rec_gll, P->rec_gll, (size_t)P->nrec));
   TRY(dalloc(h, (void **)&h->traces, (size_t)trace_capacity * 7 * P->nrec * 8));
   TRY(dalloc(h, (void **)&h->norm_part, 6 * 1024 * 8));
+  TRY(dzero(h, (void **)&h->err_dev, sizeof(int)));
+
+  if (precision == SE2GPU_FP64) {
+    const size_t vbytes = (size_t)nnodes * 2 * 8;
+    for (int b = 0; b < 2; b++)
+      for (int f = 0; f < 3; f++) TRY(dzero(h, &h->f64[b][f], vbytes));
+    TRY(upload(h, &h->mass, P->mass, (size_t)nnodes));   // the reference divides by M
+  } else {
+    const bool kahan = (precision == SE2GPU_FP32_KAHAN);
+    h->pitch = (int)((nx_g + 15) / 16 * 16);
+    const size_t np = (size_t)ny_g * h->pitch;
+    for (int b = 0; b < 2; b++) {
+      TRY(dzero(h, (void **)&h->pu[b], np * 8));
+      TRY(dzero(h, (void **)&h->pw[b], np * 8));
+      if (kahan) { TRY(dzero(h, (void **)&h->pcu[b], np * 8)); TRY(dzero(h, (void **)&h->pcw[b], np * 8)); }
+      TRY(dzero(h, (void **)&h->rbuf[b], (size_t)P->nrec * npe * 6 * 4));
+    }
+    TRY(dzero(h, (void **)&h->pa, np * 8));
+    {
+      std::vector<float> minv(np, 0.f);
+      for (long y = 0; y < ny_g; y++)
+        for (long x = 0; x < nx_g; x++) minv[(size_t)(y * h->pitch + x)] = (float)(1.0 / P->mass[y * nx_g + x]);
+      TRY(dalloc(h, (void **)&h->pminv, np * 4));
+      if (cudaMemcpy(h->pminv, minv.data(), np * 4, cudaMemcpyHostToDevice) != cudaSuccess) { fail(h, SE2GPU_ERR_CUDA, "upload 1/M"); TRY(SE2GPU_ERR_CUDA); }
+    }
+    {
+      cudaError_t e = se2p::set_tables(P->p, P->D, P->w1d);
+      if (e != cudaSuccess) { fail(h, SE2GPU_ERR_CUDA, "constant tables: %s", cudaGetErrorString(e)); TRY(SE2GPU_ERR_CUDA); }
+      h->src_elem_h = new std::vector<int>(P->src_elem, P->src_elem + P->nsrc);
+      h->rec_elem_h = new std::vector<int>(P->rec_elem, P->rec_elem + P->nrec);
+      TRY(setup_f32_config(h, 0));
+    }
+  }
 #undef TRY
   *out = h;
   return 0;
@@ -216,67 +359,86 @@ extern "C" int se2gpu_set_stream(se2gpu_solver *h, void *stream)
   return 0;
 }
 
+static int check_err_flag(se2gpu_solver *h)
+{
+  int flag = 0;
+  CK(h, cudaMemcpy(&flag, h->err_dev, sizeof(int), cudaMemcpyDeviceToHost));
+  if (flag) return fail(h, SE2GPU_ERR_CUDA, "a step kernel gave up waiting for its tile copies (bounded wait expired)");
+  return 0;
+}
+
 extern "C" int se2gpu_synchronize(se2gpu_solver *h)
 {
   if (!h) return SE2GPU_ERR_ARG;
   CK(h, cudaStreamSynchronize(h->stream));
-  return 0;
+  return check_err_flag(h);
 }
 
-template <typename T>
-static se2::StepParams<T> base_params(se2gpu_solver *h)
+// ---------------------------------------------------------------- FP64 (tiled, reference order)
+static se2::StepParams<double> f64_params(se2gpu_solver *h)
 {
-  se2::StepParams<T> prm;
+  se2::StepParams<double> prm;
   memset(&prm, 0, sizeof(prm));
   prm.mx = h->mx; prm.my = h->my; prm.nx_g = h->nx_g; prm.ny_g = h->ny_g;
   prm.ntx = h->ntx; prm.nty = h->nty;
-  prm.mass = (const T *)h->mass; prm.lam = (const T *)h->lam; prm.mu = (const T *)h->mu;
-  prm.J00 = (const T *)h->J00; prm.J11 = (const T *)h->J11; prm.iJ00 = (const T *)h->iJ00; prm.iJ11 = (const T *)h->iJ11;
-  prm.D = (const T *)h->D; prm.wq = (const T *)h->wq;
+  prm.mass = (const double *)h->mass; prm.lam = (const double *)h->lam; prm.mu = (const double *)h->mu;
+  prm.J00 = (const double *)h->J00; prm.J11 = (const double *)h->J11;
+  prm.iJ00 = (const double *)h->iJ00; prm.iJ11 = (const double *)h->iJ11;
+  prm.D = (const double *)h->D; prm.wq = (const double *)h->wq;
   // coefficients exactly as the reference forms them: dt, 0.5*dt*dt, 0.5*dt
-  prm.c_dt = (T)h->dt; prm.c_u = (T)(0.5 * h->dt * h->dt); prm.c_v = (T)(0.5 * h->dt);
-  prm.nsrc = h->nsrc; prm.src_elem = h->src_elem; prm.src_vals = (const T *)h->src_vals;
+  prm.c_dt = h->dt; prm.c_u = 0.5 * h->dt * h->dt; prm.c_v = 0.5 * h->dt;
+  prm.nsrc = h->nsrc; prm.src_elem = h->src_elem; prm.src_vals = (const double *)h->src_vals;
   prm.nrec = h->nrec; prm.rec_node = h->rec_node; prm.rec_elem = h->rec_elem; prm.rec_gll = h->rec_gll;
   prm.Dd = h->Dd; prm.iJ00d = h->iJ00d; prm.iJ11d = h->iJ11d;
   return prm;
 }
 
-template <typename T>
-static void bind_state(se2gpu_solver *h, se2::StepParams<T> &prm, int in, int outb)
+static void f64_bind(se2gpu_solver *h, se2::StepParams<double> &prm, int in, int outb)
 {
-  typedef typename se2::Vec2<T>::type T2;
-  prm.u_in = (const T2 *)h->fields[in][0]; prm.v_in = (const T2 *)h->fields[in][1]; prm.a_in = (const T2 *)h->fields[in][2];
-  prm.cu_in = (const T2 *)h->fields[in][3]; prm.cv_in = (const T2 *)h->fields[in][4];
-  prm.u_out = (T2 *)h->fields[outb][0]; prm.v_out = (T2 *)h->fields[outb][1]; prm.a_out = (T2 *)h->fields[outb][2];
-  prm.cu_out = (T2 *)h->fields[outb][3]; prm.cv_out = (T2 *)h->fields[outb][4];
+  prm.u_in = (const double2 *)h->f64[in][0]; prm.v_in = (const double2 *)h->f64[in][1]; prm.a_in = (const double2 *)h->f64[in][2];
+  prm.u_out = (double2 *)h->f64[outb][0]; prm.v_out = (double2 *)h->f64[outb][1]; prm.a_out = (double2 *)h->f64[outb][2];
 }
 
-static cudaError_t launch_step(se2gpu_solver *h, const void *prm, int nblocks)
+// ---------------------------------------------------------------- FP32 (persistent leapfrog)
+static se2p::Params f32_params(se2gpu_solver *h)
 {
-  h->launches++;
-  if (h->precision == SE2GPU_FP64)
-    return se2::launch_step_f64(h->p, *(const se2::StepParams<double> *)prm, nblocks, h->stream);
-  return se2::launch_step_f32(h->p, h->precision == SE2GPU_FP32_KAHAN, *(const se2::StepParams<float> *)prm, nblocks, h->stream);
+  se2p::Params prm;
+  memset(&prm, 0, sizeof(prm));
+  prm.mx = h->mx; prm.my = h->my; prm.nx_g = h->nx_g; prm.ny_g = h->ny_g; prm.pitch = h->pitch;
+  prm.ntx = h->pntx; prm.nty = h->pnty; prm.ntiles = h->pntx * h->pnty;
+  prm.minv = h->pminv;
+  prm.lam = (const float *)h->lam; prm.mu = (const float *)h->mu;
+  prm.J00 = (const float *)h->J00; prm.J11 = (const float *)h->J11;
+  prm.iJ00 = (const float *)h->iJ00; prm.iJ11 = (const float *)h->iJ11;
+  prm.dt = (float)h->dt; prm.half_dt = (float)(0.5 * h->dt);
+  prm.nsrc = h->nsrc; prm.src_elem = h->src_elem; prm.src_vals = (const float *)h->src_vals;
+  prm.nrec = h->nrec; prm.rec_elem = h->rec_elem; prm.rec_gll = h->rec_gll;
+  prm.Dd = h->Dd; prm.iJ00d = h->iJ00d; prm.iJ11d = h->iJ11d;
+  prm.err = h->err_dev;
+  prm.tile_src_off = h->tile_src_off; prm.tile_src_idx = h->tile_src_idx;
+  prm.tile_rec_off = h->tile_rec_off; prm.tile_rec_idx = h->tile_rec_idx;
+  return prm;
 }
 
-// record the receivers of the current state if a step left its row pending
+// record the receivers of the last step if its row is still pending
 static int flush_record(se2gpu_solver *h)
 {
   if (!h->pending_record) return 0;
   cudaError_t e;
   h->launches++;
-  if (h->precision == SE2GPU_FP64) {
-    auto prm = base_params<double>(h);
-    bind_state(h, prm, h->cur, h->cur);
+  double *row = h->traces + (size_t)h->rows_written * 7 * h->nrec;
+  if (is_f64(h)) {
+    auto prm = f64_params(h);
+    f64_bind(h, prm, h->cur, h->cur);
     prm.record = 1;
-    prm.trace_row = h->traces + (size_t)h->rows_written * 7 * h->nrec;
+    prm.trace_row = row;
     e = se2::launch_record_f64(h->p, prm, h->stream);
   } else {
-    auto prm = base_params<float>(h);
-    bind_state(h, prm, h->cur, h->cur);
+    auto prm = f32_params(h);
+    prm.rbuf_in = h->rbuf[h->rlast];
     prm.record = 1;
-    prm.trace_row = h->traces + (size_t)h->rows_written * 7 * h->nrec;
-    e = se2::launch_record_f32(h->p, prm, h->stream);
+    prm.trace_row = row;
+    e = se2p::launch_record(h->p, prm, h->stream);
   }
   if (e != cudaSuccess) return fail(h, SE2GPU_ERR_CUDA, "receiver kernel: %s", cudaGetErrorString(e));
   h->rows_written++;
@@ -284,20 +446,44 @@ static int flush_record(se2gpu_solver *h)
   return 0;
 }
 
-template <typename T>
-static int advance_t(se2gpu_solver *h, int nsteps)
+static int advance_f64(se2gpu_solver *h, int nsteps)
 {
-  auto prm = base_params<T>(h);
+  auto prm = f64_params(h);
   prm.mode = 0;
   for (int k = 0; k < nsteps; k++) {
-    bind_state(h, prm, h->cur, 1 - h->cur);
+    f64_bind(h, prm, h->cur, 1 - h->cur);
     prm.stf = h->stf_dev + (size_t)k * h->nsrc;
     prm.record = h->pending_record ? 1 : 0;
     prm.trace_row = h->traces + (size_t)h->rows_written * 7 * h->nrec;
-    cudaError_t e = launch_step(h, &prm, h->nblocks);
+    h->launches++;
+    cudaError_t e = se2::launch_step_f64(h->p, prm, h->nblocks, h->stream);
     if (e != cudaSuccess) return fail(h, SE2GPU_ERR_CUDA, "step kernel: %s", cudaGetErrorString(e));
     if (h->pending_record) { h->rows_written++; h->pending_record = false; }
     h->cur = 1 - h->cur;
+    if (h->nrec > 0) h->pending_record = true;
+  }
+  return 0;
+}
+
+static int advance_f32(se2gpu_solver *h, int nsteps)
+{
+  auto prm = f32_params(h);
+  const bool kahan = is_kahan(h);
+  for (int k = 0; k < nsteps; k++) {
+    const int in = h->cur, outb = 1 - h->cur;
+    prm.u_out = h->pu[outb]; prm.w_out = h->pw[outb]; prm.cu_out = h->pcu[outb]; prm.cw_out = h->pcw[outb];
+    prm.a_out = (k == nsteps - 1) ? h->pa : nullptr;
+    prm.stf = h->stf_dev + (size_t)k * h->nsrc;
+    prm.rbuf_in = h->rbuf[h->rlast];
+    prm.rbuf_out = h->rbuf[1 - h->rlast];
+    prm.record = h->pending_record ? 1 : 0;
+    prm.trace_row = h->traces + (size_t)h->rows_written * 7 * h->nrec;
+    h->launches++;
+    cudaError_t e = se2p::launch_step(h->p, h->pconfig, kahan, h->maps[in], prm, h->pgrid, h->stream);
+    if (e != cudaSuccess) return fail(h, SE2GPU_ERR_CUDA, "step kernel: %s", cudaGetErrorString(e));
+    if (h->pending_record) { h->rows_written++; h->pending_record = false; }
+    h->cur = outb;
+    h->rlast = 1 - h->rlast;
     if (h->nrec > 0) h->pending_record = true;
   }
   return 0;
@@ -325,7 +511,7 @@ extern "C" int se2gpu_advance(se2gpu_solver *h, int nsteps, const double *stf)
     // the previous block may still read stf_dev: order the copy on the stream
     CK(h, cudaMemcpyAsync(h->stf_dev, stf, (size_t)nsteps * h->nsrc * 8, cudaMemcpyHostToDevice, h->stream));
   }
-  return (h->precision == SE2GPU_FP64) ? advance_t<double>(h, nsteps) : advance_t<float>(h, nsteps);
+  return is_f64(h) ? advance_f64(h, nsteps) : advance_f32(h, nsteps);
 }
 
 extern "C" int se2gpu_traces(se2gpu_solver *h, double *out, int max_rows)
@@ -343,6 +529,7 @@ extern "C" int se2gpu_traces(se2gpu_solver *h, double *out, int max_rows)
   }
   CK(h, cudaStreamSynchronize(h->stream));
   CK(h, cudaGetLastError());
+  if ((rc = check_err_flag(h))) return rc;
   h->rows_written = 0;
   return rows;
 }
@@ -355,22 +542,19 @@ extern "C" int se2gpu_set_fields(se2gpu_solver *h, const double *u, const double
   if (rc) return rc;
   CK(h, cudaStreamSynchronize(h->stream));
   const size_t n = (size_t)h->nnodes * 2;
-  const double *src[3] = {u, v, a};
-  for (int f = 0; f < 3; f++) {
-    if (!src[f]) continue;
-    if (h->tsize == 8) {
-      CK(h, cudaMemcpy(h->fields[h->cur][f], src[f], n * 8, cudaMemcpyHostToDevice));
-    } else {
-      std::vector<float> tmp(n);
-      for (size_t i = 0; i < n; i++) tmp[i] = (float)src[f][i];
-      CK(h, cudaMemcpy(h->fields[h->cur][f], tmp.data(), n * 4, cudaMemcpyHostToDevice));
-    }
+  if (is_f64(h)) {
+    const double *src[3] = {u, v, a};
+    for (int f = 0; f < 3; f++)
+      if (src[f]) CK(h, cudaMemcpy(h->f64[h->cur][f], src[f], n * 8, cudaMemcpyHostToDevice));
+    return 0;
   }
-  if (h->precision == SE2GPU_FP32_KAHAN) {
-    CK(h, cudaMemset(h->fields[h->cur][3], 0, n * 4));
-    CK(h, cudaMemset(h->fields[h->cur][4], 0, n * 4));
+  // FP32: unspecified fields keep their current values
+  if (!u || !v || !a) {
+    std::vector<double> cu(n), cv(n), ca(n);
+    if ((rc = se2gpu_get_fields(h, cu.data(), cv.data(), ca.data()))) return rc;
+    return upload_leapfrog(h, u ? u : cu.data(), v ? v : cv.data(), a ? a : ca.data());
   }
-  return 0;
+  return upload_leapfrog(h, u, v, a);
 }
 
 extern "C" int se2gpu_get_fields(se2gpu_solver *h, double *u, double *v, double *a)
@@ -378,18 +562,35 @@ extern "C" int se2gpu_get_fields(se2gpu_solver *h, double *u, double *v, double 
   if (!h) return SE2GPU_ERR_ARG;
   CK(h, cudaSetDevice(h->device));
   CK(h, cudaStreamSynchronize(h->stream));
+  int rc;
+  if ((rc = check_err_flag(h))) return rc;
   const size_t n = (size_t)h->nnodes * 2;
-  double *dst[3] = {u, v, a};
-  for (int f = 0; f < 3; f++) {
-    if (!dst[f]) continue;
-    if (h->tsize == 8) {
-      CK(h, cudaMemcpy(dst[f], h->fields[h->cur][f], n * 8, cudaMemcpyDeviceToHost));
-    } else {
-      std::vector<float> tmp(n);
-      CK(h, cudaMemcpy(tmp.data(), h->fields[h->cur][f], n * 4, cudaMemcpyDeviceToHost));
-      for (size_t i = 0; i < n; i++) dst[f][i] = (double)tmp[i];
-    }
+  if (is_f64(h)) {
+    double *dst[3] = {u, v, a};
+    for (int f = 0; f < 3; f++)
+      if (dst[f]) CK(h, cudaMemcpy(dst[f], h->f64[h->cur][f], n * 8, cudaMemcpyDeviceToHost));
+    return 0;
   }
+  const size_t np = (size_t)h->ny_g * h->pitch;
+  std::vector<float2> U(np), W(np), CU(np, make_float2(0.f, 0.f)), CW(np, make_float2(0.f, 0.f)), A(np);
+  const int c = h->cur;
+  CK(h, cudaMemcpy(U.data(), h->pu[c], np * 8, cudaMemcpyDeviceToHost));
+  CK(h, cudaMemcpy(W.data(), h->pw[c], np * 8, cudaMemcpyDeviceToHost));
+  if (is_kahan(h)) {
+    CK(h, cudaMemcpy(CU.data(), h->pcu[c], np * 8, cudaMemcpyDeviceToHost));
+    CK(h, cudaMemcpy(CW.data(), h->pcw[c], np * 8, cudaMemcpyDeviceToHost));
+  }
+  CK(h, cudaMemcpy(A.data(), h->pa, np * 8, cudaMemcpyDeviceToHost));
+  const double dt = h->dt, hdt = 0.5 * h->dt;
+  for (long y = 0; y < h->ny_g; y++)
+    for (long x = 0; x < h->nx_g; x++) {
+      const size_t nn = (size_t)(y * h->nx_g + x), k = (size_t)(y * h->pitch + x);
+      const double w0 = (double)W[k].x - (double)CW[k].x, w1 = (double)W[k].y - (double)CW[k].y;
+      const double u0 = (double)U[k].x - (double)CU[k].x, u1 = (double)U[k].y - (double)CU[k].y;
+      if (u) { u[2 * nn] = u0 - dt * w0; u[2 * nn + 1] = u1 - dt * w1; }
+      if (v) { v[2 * nn] = w0 - hdt * (double)A[k].x; v[2 * nn + 1] = w1 - hdt * (double)A[k].y; }
+      if (a) { a[2 * nn] = (double)A[k].x; a[2 * nn + 1] = (double)A[k].y; }
+    }
   return 0;
 }
 
@@ -397,17 +598,22 @@ extern "C" int se2gpu_norms(se2gpu_solver *h, double out[6])
 {
   if (!h || !out) return SE2GPU_ERR_ARG;
   CK(h, cudaSetDevice(h->device));
-  const long n = h->nnodes * 2;
   const int nb = 1024;
   h->launches++;
-  if (h->tsize == 8)
-    se2::norms_partial<double><<<nb, 256, 0, h->stream>>>((const double *)h->fields[h->cur][0], (const double *)h->fields[h->cur][1], n, h->norm_part);
-  else
-    se2::norms_partial<float><<<nb, 256, 0, h->stream>>>((const float *)h->fields[h->cur][0], (const float *)h->fields[h->cur][1], n, h->norm_part);
-  CK(h, cudaGetLastError());
+  if (is_f64(h)) {
+    se2::norms_partial<double><<<nb, 256, 0, h->stream>>>((const double *)h->f64[h->cur][0], (const double *)h->f64[h->cur][1],
+                                                          h->nnodes * 2, h->norm_part);
+    CK(h, cudaGetLastError());
+  } else {
+    CK(h, se2p::launch_norms(h->pu[h->cur], h->pw[h->cur], is_kahan(h) ? h->pcu[h->cur] : nullptr,
+                             is_kahan(h) ? h->pcw[h->cur] : nullptr, h->pa, h->nx_g, h->ny_g, h->pitch, h->dt,
+                             h->norm_part, nb, h->stream));
+  }
   std::vector<double> part(6 * nb);
   CK(h, cudaMemcpyAsync(part.data(), h->norm_part, part.size() * 8, cudaMemcpyDeviceToHost, h->stream));
   CK(h, cudaStreamSynchronize(h->stream));
+  int rc;
+  if ((rc = check_err_flag(h))) return rc;
   double r[6] = {-1.0e308, 1.0e308, 0.0, -1.0e308, 1.0e308, 0.0};
   for (int b = 0; b < nb; b++) {
     r[0] = std::fmax(r[0], part[6 * b + 0]); r[1] = std::fmin(r[1], part[6 * b + 1]); r[2] += part[6 * b + 2];
@@ -420,16 +626,23 @@ extern "C" int se2gpu_norms(se2gpu_solver *h, double out[6])
   return 0;
 }
 
+// ---------------------------------------------------------------- internal force (packed layout)
 template <typename T>
 static int force_t(se2gpu_solver *h, const void *u_dev, void *F_dev)
 {
   typedef typename se2::Vec2<T>::type T2;
-  auto prm = base_params<T>(h);
+  se2::StepParams<T> prm;
+  memset(&prm, 0, sizeof(prm));
+  prm.mx = h->mx; prm.my = h->my; prm.nx_g = h->nx_g; prm.ny_g = h->ny_g; prm.ntx = h->ntx; prm.nty = h->nty;
+  prm.lam = (const T *)h->lam; prm.mu = (const T *)h->mu; prm.J00 = (const T *)h->J00; prm.J11 = (const T *)h->J11;
+  prm.iJ00 = (const T *)h->iJ00; prm.iJ11 = (const T *)h->iJ11; prm.D = (const T *)h->D; prm.wq = (const T *)h->wq;
   prm.mode = 1;
   prm.u_in = (const T2 *)u_dev;
   prm.f_out = (T2 *)F_dev;
-  prm.record = 0;
-  cudaError_t e = launch_step(h, &prm, h->nblocks - 1);
+  h->launches++;
+  cudaError_t e;
+  if constexpr (sizeof(T) == 8) e = se2::launch_step_f64(h->p, prm, h->nblocks - 1, h->stream);
+  else e = se2::launch_step_f32(h->p, false, prm, h->nblocks - 1, h->stream);
   if (e != cudaSuccess) return fail(h, SE2GPU_ERR_CUDA, "force kernel: %s", cudaGetErrorString(e));
   return 0;
 }
@@ -474,14 +687,47 @@ extern "C" int se2gpu_info(const se2gpu_solver *h, long *ints)
   if (!h || !ints) return SE2GPU_ERR_ARG;
   ints[0] = h->nx_g; ints[1] = h->ny_g; ints[2] = h->p; ints[3] = h->precision;
   ints[4] = h->nsrc; ints[5] = h->nrec; ints[6] = h->launches; ints[7] = h->rows_written + (h->pending_record ? 1 : 0);
+  ints[8] = is_f64(h) ? h->nx_g : h->pitch;
   return 0;
 }
 
 extern "C" int se2gpu_device_fields(const se2gpu_solver *h, void **u, void **v, void **a)
 {
   if (!h) return SE2GPU_ERR_ARG;
-  if (u) *u = h->fields[h->cur][0];
-  if (v) *v = h->fields[h->cur][1];
-  if (a) *a = h->fields[h->cur][2];
+  if (is_f64(h)) {
+    if (u) *u = h->f64[h->cur][0];
+    if (v) *v = h->f64[h->cur][1];
+    if (a) *a = h->f64[h->cur][2];
+  } else {
+    if (u) *u = h->pu[h->cur];
+    if (v) *v = h->pw[h->cur];
+    if (a) *a = h->pa;
+  }
   return 0;
+}
+
+extern "C" int se2gpu_tile_configs(const se2gpu_solver *h, int *edge, int *threads, int max_configs)
+{
+  if (!h) return SE2GPU_ERR_ARG;
+  if (is_f64(h)) {
+    if (max_configs > 0 && edge && threads) { edge[0] = se2::tile_edge(h->p); threads[0] = 256; }
+    return 1;
+  }
+  const int n = se2p::num_configs(h->p);
+  for (int c = 0; c < n && c < max_configs; c++) {
+    se2p::TileShape ts;
+    se2p::config_shape(h->p, c, is_kahan(h), &ts);
+    if (edge) edge[c] = ts.tex;
+    if (threads) threads[c] = ts.nt;
+  }
+  return n;
+}
+
+extern "C" int se2gpu_set_tile_config(se2gpu_solver *h, int config)
+{
+  if (!h) return SE2GPU_ERR_ARG;
+  if (is_f64(h)) return (config == 0) ? 0 : fail(h, SE2GPU_ERR_ARG, "FP64 mode has a single tile configuration");
+  if (config < 0 || config >= se2p::num_configs(h->p)) return fail(h, SE2GPU_ERR_ARG, "tile configuration %d out of range", config);
+  CK(h, cudaSetDevice(h->device));
+  return setup_f32_config(h, config);
 }

@@ -1,0 +1,206 @@
+// se2gpu_f32p.cu -- persistent TMA-pipelined FP32 kernels (plain / Kahan), degrees 1..8,
+// the tile configurations the autotuner chooses from, and their host-side helpers
+// (tensor maps, constant tables, norms of the leapfrog state).
+#include <cudaTypedefs.h>
+
+#include "se2gpu_persist.cuh"
+#include "se2gpu_persist_launch.h"
+
+namespace se2p {
+
+cudaError_t set_tables(int p, const double *D, const double *w1d)
+{
+  float d[81] = {0}, w[9] = {0};
+  const int n1 = p + 1;
+  for (int i = 0; i < n1 * n1; i++) d[i] = (float)D[i];
+  for (int i = 0; i < n1; i++) w[i] = (float)w1d[i];
+  cudaError_t e = cudaMemcpyToSymbol(c_D, d, sizeof(d), sizeof(d) * (p - 1));
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyToSymbol(c_w, w, sizeof(w), sizeof(w) * (p - 1));
+}
+
+// ---- one configuration = (degree, elements per tile edge, threads) ----------
+struct Entry {
+  int p, te, nt;
+  size_t smem[2];                 // [kahan]
+  const void *fn[2];              // persist_step<...> [kahan]
+};
+
+template <int P, int TE, int NT, bool K>
+static constexpr int min_blocks() { return (2 * (Layout<P, TE, K>::TOTAL + 1024) <= 233472) ? 2 : 1; }
+
+template <int P, int TE, int NT>
+static Entry entry()
+{
+  Entry e;
+  e.p = P; e.te = TE; e.nt = NT;
+  e.smem[0] = Layout<P, TE, false>::TOTAL;
+  e.smem[1] = Layout<P, TE, true>::TOTAL;
+  e.fn[0] = (const void *)persist_step<P, TE, NT, false>;
+  e.fn[1] = (const void *)persist_step<P, TE, NT, true>;
+  return e;
+}
+
+// every (element, line) item of a tile gets its own thread: NT >= (TE+1)^2 (P+1)
+static const Entry *table(int *n)
+{
+  static Entry t[] = {
+      entry<1, 15, 512>(), entry<1, 11, 288>(),
+      entry<2, 10, 384>(), entry<2, 8, 256>(),
+      entry<3, 8, 352>(),  entry<3, 7, 256>(),
+      entry<4, 7, 320>(),  entry<4, 6, 256>(), entry<4, 8, 416>(),
+      entry<5, 6, 320>(),  entry<5, 5, 224>(),
+      entry<6, 5, 256>(),  entry<6, 4, 192>(),
+      entry<7, 5, 288>(),  entry<7, 4, 224>(),
+      entry<8, 4, 256>(),  entry<8, 3, 160>(),
+  };
+  *n = (int)(sizeof(t) / sizeof(t[0]));
+  return t;
+}
+
+static const Entry *find(int p, int config)
+{
+  int n, k = 0;
+  const Entry *t = table(&n);
+  for (int i = 0; i < n; i++)
+    if (t[i].p == p) {
+      if (k == config) return &t[i];
+      k++;
+    }
+  return nullptr;
+}
+
+int num_configs(int p)
+{
+  int n, k = 0;
+  const Entry *t = table(&n);
+  for (int i = 0; i < n; i++) k += (t[i].p == p);
+  return k;
+}
+
+int config_shape(int p, int config, bool kahan, TileShape *s)
+{
+  const Entry *e = find(p, config);
+  if (!e) return -1;
+  s->tex = s->tey = e->te;
+  s->nt = e->nt;
+  s->region_w = round_up((e->te + 1) * p + 2, 2);
+  s->region_h = (e->te + 1) * p + 1;
+  s->own_w = round_up(e->te * p + 2, 2);
+  s->own_h = e->te * p + 1;
+  s->smem = e->smem[kahan ? 1 : 0];
+  return 0;
+}
+
+cudaError_t prepare(int p, int config, bool kahan)
+{
+  const Entry *e = find(p, config);
+  if (!e) return cudaErrorInvalidValue;
+  const void *fn = e->fn[kahan ? 1 : 0];
+  cudaError_t r = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem[kahan ? 1 : 0]);
+  if (r != cudaSuccess) return r;
+  return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+}
+
+int occupancy(int p, int config, bool kahan)
+{
+  const Entry *e = find(p, config);
+  int n = 0;
+  if (!e || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, e->fn[kahan ? 1 : 0], e->nt, e->smem[kahan ? 1 : 0]) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  return n;
+}
+
+cudaError_t launch_step(int p, int config, bool kahan, const CUtensorMap *maps, const Params &prm, int grid,
+                        cudaStream_t st)
+{
+  const Entry *e = find(p, config);
+  if (!e) return cudaErrorInvalidValue;
+  Params pc = prm;
+  CUtensorMap m0 = maps[0], m1 = maps[1], m2 = maps[2], m3 = maps[3];
+  void *args[] = {&m0, &m1, &m2, &m3, &pc};
+  return cudaLaunchKernel(e->fn[kahan ? 1 : 0], dim3(grid), dim3(e->nt), args, e->smem[kahan ? 1 : 0], st);
+}
+
+template <int P>
+static cudaError_t record_t(const Params &prm, cudaStream_t st)
+{
+  persist_record<P><<<1, 128, 0, st>>>(prm);
+  return cudaGetLastError();
+}
+cudaError_t launch_record(int p, const Params &prm, cudaStream_t st)
+{
+  switch (p) {
+    case 1: return record_t<1>(prm, st); case 2: return record_t<2>(prm, st);
+    case 3: return record_t<3>(prm, st); case 4: return record_t<4>(prm, st);
+    case 5: return record_t<5>(prm, st); case 6: return record_t<6>(prm, st);
+    case 7: return record_t<7>(prm, st); case 8: return record_t<8>(prm, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// tensor map of one padded float2 field, box (bw, bh) nodes
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+int make_map(CUtensorMap *map, void *base, int nx, int ny, int pitch, int bw, int bh)
+{
+  if (!g_encode) {
+    cudaDriverEntryPointQueryResult q;
+    void *fn = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+      return -1;
+    g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  }
+  cuuint64_t dims[2] = {(cuuint64_t)nx, (cuuint64_t)ny};
+  cuuint64_t strides[1] = {(cuuint64_t)pitch * 8};
+  cuuint32_t box[2] = {(cuuint32_t)bw, (cuuint32_t)bh};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, base, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? 0 : -(int)r - 1000;
+}
+
+// norms of (u_k, v_k) recovered from the leapfrog state in FP64:
+// u_k = (u - cu) - dt (w - cw),  v_k = (w - cw) - dt/2 a_k
+__global__ void norms_leapfrog(const float2 *u, const float2 *w, const float2 *cu, const float2 *cw, const float2 *a,
+                               int nx, int ny, int pitch, double dt, double half_dt, double *part)
+{
+  __shared__ double s[6][256];
+  double umax = -1.0e308, umin = 1.0e308, uss = 0.0, vmax = -1.0e308, vmin = 1.0e308, vss = 0.0;
+  const long n = (long)nx * ny;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const long y = i / nx, x = i - y * nx, k = y * pitch + x;
+    const float2 uu = u[k], ww = w[k], aa = a[k];
+    const float2 cuu = cu ? cu[k] : make_float2(0.f, 0.f), cww = cw ? cw[k] : make_float2(0.f, 0.f);
+    const double wx = (double)ww.x - (double)cww.x, wy = (double)ww.y - (double)cww.y;
+    const double ux = ((double)uu.x - (double)cuu.x) - dt * wx, uy = ((double)uu.y - (double)cuu.y) - dt * wy;
+    const double vx = wx - half_dt * (double)aa.x, vy = wy - half_dt * (double)aa.y;
+    umax = fmax(umax, fmax(ux, uy)); umin = fmin(umin, fmin(ux, uy)); uss += ux * ux + uy * uy;
+    vmax = fmax(vmax, fmax(vx, vy)); vmin = fmin(vmin, fmin(vx, vy)); vss += vx * vx + vy * vy;
+  }
+  s[0][threadIdx.x] = umax; s[1][threadIdx.x] = umin; s[2][threadIdx.x] = uss;
+  s[3][threadIdx.x] = vmax; s[4][threadIdx.x] = vmin; s[5][threadIdx.x] = vss;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) {
+      const int t = threadIdx.x;
+      s[0][t] = fmax(s[0][t], s[0][t + h]); s[1][t] = fmin(s[1][t], s[1][t + h]); s[2][t] += s[2][t + h];
+      s[3][t] = fmax(s[3][t], s[3][t + h]); s[4][t] = fmin(s[4][t], s[4][t + h]); s[5][t] += s[5][t + h];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 6) part[blockIdx.x * 6 + threadIdx.x] = s[threadIdx.x][0];
+}
+
+cudaError_t launch_norms(const float2 *u, const float2 *w, const float2 *cu, const float2 *cw, const float2 *a, int nx,
+                         int ny, int pitch, double dt, double *part, int nblocks, cudaStream_t st)
+{
+  norms_leapfrog<<<nblocks, 256, 0, st>>>(u, w, cu, cw, a, nx, ny, pitch, dt, 0.5 * dt, part);
+  return cudaGetLastError();
+}
+
+}  // namespace se2p

@@ -1,0 +1,437 @@
+// se2gpu_persist.cuh -- persistent, TMA-pipelined FP32 step kernel for sm_103a.
+//
+// FP32 modes advance the same explicit Newmark (beta = 0, gamma = 1/2) scheme as
+// se2wave.c:4722-4775, written as kick-drift leapfrog so that a step needs the
+// neighbours' displacement only:
+//
+//   state before step k: u_k, w_k = v_{k-1} + dt/2 a_{k-1}          (half-step velocity)
+//   a_k     = M^-1 (K u_k + sum_s stf_s(t_k) g_s)
+//   v_k     = w_k + dt/2 a_k                                        (recorded at receivers)
+//   w_{k+1} = w_k + dt a_k,   u_{k+1} = u_k + dt w_{k+1}             (Kahan-compensated)
+//
+// which is algebraically identical to the reference's u += dt v + dt^2/2 a,
+// v += dt/2 a, a = f/M, v += dt/2 a.  Per node and step the kernel reads u, w
+// (+ compensations cu, cw) and writes them back: 68.5 B/node with Kahan terms.
+//
+// Execution: a persistent grid (CTAs resident on every SM) walks the tiles.  A
+// tile is TE x TE elements; its CTA owns their nodes except the line shared
+// with the next tile, and recomputes the one-element halo column/row on its
+// left/bottom whose forces reach its boundary nodes.  Thread 0 issues 2-D TMA
+// bulk-tensor copies of the next tile's node region (u, cu) and owned nodes
+// (w, cw) into the second shared-memory stage, signalled through an mbarrier,
+// while all threads compute the current tile.  Every wait is bounded: on
+// timeout the CTA records an error code, waits (bounded) for its own copies and
+// returns.
+//
+// Per tile, one thread per (element, line j) -- NT covers every item, so all
+// per-item values stay in registers between the three phases:
+//   1. along row j: d/dxi at the row's GLL points; along column j: d/deta at
+//      the column's points (to shared memory).  Derivatives are taken of the
+//      compensated displacement relative to the line's first node,
+//      (u_k - u_0) - (cu_k - cu_0): differences of nearby values are exact, so
+//      the derivative of a smooth field loses no digits to cancellation;
+//   2. Hooke stress at the row's points, scaled by -detJ w_q; the xi part of
+//      the weak divergence from registers, the eta fluxes to shared memory;
+//   3. the eta part of the divergence for the row's nodes; element forces to
+//      shared memory.
+// Then one thread per owned node sums the 1, 2 or 4 element contributions in a
+// fixed order (deterministic, no atomics), adds the sources and updates.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "se2gpu_persist_params.h"
+
+namespace se2p {
+
+// FP32 derivative matrix and GLL weights per degree, in constant memory so that
+// compile-time indices become constant-bank operands (this header is compiled
+// into one translation unit only)
+__constant__ float c_D[8][81];
+__constant__ float c_w[8][9];
+
+// ---------------------------------------------------------------- PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
+{
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void fence_barrier_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar)
+{
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(dst), "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void prefetch_map(const CUtensorMap *map)
+{
+  asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)map) : "memory");
+}
+
+// bounded wait on a tile's copies
+constexpr long WAIT_LIMIT = 1L << 24;
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity)
+{
+  for (long i = 0; i < WAIT_LIMIT; i++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// ---------------------------------------------------------------- geometry
+__host__ __device__ constexpr int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+template <int P, int TE>
+struct Geo {
+  static constexpr int N1 = P + 1, NPE = N1 * N1;
+  static constexpr int NEX = TE + 1, NE = NEX * NEX;      // elements incl. halo
+  static constexpr int ITEMS = NE * N1;                   // (element, line) work items
+  // region box (u, cu): the x start is rounded down to an even node so the copy
+  // starts on a 16-byte boundary; one extra column absorbs the shift
+  static constexpr int BXW = round_up(NEX * P + 2, 2);
+  static constexpr int BXH = NEX * P + 1;
+  static constexpr int OWM = TE * P + 1;                  // owned nodes per row (max)
+  static constexpr int OBW = round_up(OWM + 1, 2);        // owned box (w, cw)
+  static constexpr int OBH = OWM;
+};
+
+__host__ __device__ constexpr size_t al128(size_t x) { return (x + 127) & ~size_t(127); }
+
+template <int P, int TE, bool KAHAN>
+struct Layout {
+  typedef Geo<P, TE> G;
+  static constexpr size_t REG = al128(sizeof(float2) * G::BXW * G::BXH);
+  static constexpr size_t OWN = al128(sizeof(float2) * G::OBW * G::OBH);
+  static constexpr size_t STAGE = (REG + OWN) * (KAHAN ? 2 : 1);
+  static constexpr size_t XCH = al128(sizeof(float2) * G::NE * G::NPE);   // exchange buffer
+  static constexpr size_t MISC = 64;
+  static constexpr size_t TOTAL = 2 * STAGE + 2 * XCH + MISC;
+  static constexpr uint32_t TX_BYTES =
+      (uint32_t)((KAHAN ? 2 : 1) * (sizeof(float2) * G::BXW * G::BXH + sizeof(float2) * G::OBW * G::OBH));
+};
+
+struct TileBox {
+  int ex0, ex1, ey0, ey1, EX0, EY0, NEXa, NEYa, X0, Y0, OW, OH, RXa, RYa, OXa;
+};
+
+template <int P, int TE>
+__device__ __forceinline__ TileBox tile_box(const Params &prm, int t)
+{
+  TileBox b;
+  const int tx = t % prm.ntx, ty = t / prm.ntx;
+  b.ex0 = tx * TE; b.ex1 = min(b.ex0 + TE, prm.mx);
+  b.ey0 = ty * TE; b.ey1 = min(b.ey0 + TE, prm.my);
+  b.EX0 = max(b.ex0 - 1, 0); b.EY0 = max(b.ey0 - 1, 0);
+  b.NEXa = b.ex1 - b.EX0; b.NEYa = b.ey1 - b.EY0;
+  b.X0 = b.ex0 * P; b.Y0 = b.ey0 * P;
+  b.OW = (b.ex1 - b.ex0) * P + (b.ex1 == prm.mx ? 1 : 0);
+  b.OH = (b.ey1 - b.ey0) * P + (b.ey1 == prm.my ? 1 : 0);
+  b.RXa = (b.EX0 * P) & ~1;     // region box origin (even x)
+  b.RYa = b.EY0 * P;
+  b.OXa = b.X0 & ~1;            // owned box origin (even x)
+  return b;
+}
+
+// issue the copies of tile t into a stage
+template <int P, int TE, bool KAHAN>
+__device__ __forceinline__ void issue_tile(const Params &prm, int t, unsigned char *stage, uint32_t bar,
+                                           const CUtensorMap *tm_u, const CUtensorMap *tm_cu,
+                                           const CUtensorMap *tm_w, const CUtensorMap *tm_cw)
+{
+  typedef Layout<P, TE, KAHAN> L;
+  const TileBox b = tile_box<P, TE>(prm, t);
+  mbar_expect_tx(bar, L::TX_BYTES);
+  size_t o = 0;
+  tma_load_2d(smem_u32(stage + o), tm_u, b.RXa, b.RYa, bar); o += L::REG;
+  if (KAHAN) { tma_load_2d(smem_u32(stage + o), tm_cu, b.RXa, b.RYa, bar); o += L::REG; }
+  tma_load_2d(smem_u32(stage + o), tm_w, b.OXa, b.Y0, bar); o += L::OWN;
+  if (KAHAN) { tma_load_2d(smem_u32(stage + o), tm_cw, b.OXa, b.Y0, bar); }
+}
+
+__device__ __forceinline__ void kahan_add(float &s, float &c, float inc)
+{
+  const float y = inc - c;
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
+// receiver rows of the previous step from the side buffer (u, v, a per element node)
+template <int P>
+__device__ void sample_rows(const Params &prm)
+{
+  constexpr int N1 = P + 1, NPE = N1 * N1;
+  for (int r = threadIdx.x; r < prm.nrec; r += blockDim.x) {
+    const float *rb = prm.rbuf_in + (size_t)r * NPE * 6;
+    const int g = prm.rec_gll[r], eid = prm.rec_elem[r];
+    const int ga = g % N1, gb = g / N1, ex = eid % prm.mx, ey = eid / prm.mx;
+    double *o = prm.trace_row + 7 * r;
+    for (int c = 0; c < 6; c++) o[c] = (double)rb[g * 6 + c];
+    const double ix = prm.iJ00d[ex], iy = prm.iJ11d[ey];
+    double dvxdy = 0.0, dvydx = 0.0;
+    for (int k = 0; k < N1; k++) {
+      dvxdy += (iy * prm.Dd[gb * N1 + k]) * (double)rb[(ga + k * N1) * 6 + 2];
+      dvydx += (ix * prm.Dd[ga * N1 + k]) * (double)rb[(k + gb * N1) * 6 + 3];
+    }
+    o[6] = dvydx - dvxdy;
+  }
+}
+
+template <int P, int TE, int NT, bool KAHAN>
+__global__ void __launch_bounds__(NT, ((2 * (Layout<P, TE, KAHAN>::TOTAL + 1024) <= 233472) ? 2 : 1))
+persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ CUtensorMap tm_cu,
+             const __grid_constant__ CUtensorMap tm_w, const __grid_constant__ CUtensorMap tm_cw,
+             const Params prm)
+{
+  typedef Geo<P, TE> G;
+  typedef Layout<P, TE, KAHAN> L;
+  constexpr int N1 = G::N1, NPE = G::NPE, NEX = G::NEX, BXW = G::BXW, OBW = G::OBW, OWM = G::OWM;
+  static_assert(NT >= G::ITEMS, "one (element, line) item per thread");
+  const float *D = c_D[P - 1];
+  const float *W = c_w[P - 1];
+  extern __shared__ __align__(128) unsigned char smem[];
+  unsigned char *stage0 = smem;
+  unsigned char *stage1 = smem + L::STAGE;
+  float2 *X1 = reinterpret_cast<float2 *>(smem + 2 * L::STAGE);             // eta derivatives, then element forces
+  float2 *X2 = reinterpret_cast<float2 *>(smem + 2 * L::STAGE + L::XCH);     // eta fluxes
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * L::STAGE + 2 * L::XCH);
+  const uint32_t bar0 = smem_u32(&bars[0]), bar1 = smem_u32(&bars[1]);
+
+  if (threadIdx.x == 0) {
+    mbar_init(bar0, 1);
+    mbar_init(bar1, 1);
+    fence_barrier_init();
+    prefetch_map(&tm_u); prefetch_map(&tm_w);
+    if (KAHAN) { prefetch_map(&tm_cu); prefetch_map(&tm_cw); }
+  }
+  __syncthreads();
+  if (blockIdx.x == 0 && prm.record) sample_rows<P>(prm);
+
+  // this thread's (element, line) item, the same for every tile
+  const int item = threadIdx.x;
+  const int el = item / N1, j = item - (item / N1) * N1;
+  const int ecy = el / NEX, ecx = el - (el / NEX) * NEX;
+  float Dcj[N1];   // column j of D
+#pragma unroll
+  for (int k = 0; k < N1; k++) Dcj[k] = (item < G::ITEMS) ? D[k * N1 + j] : 0.f;
+  const float wj = (item < G::ITEMS) ? W[j] : 0.f;
+
+  int t = blockIdx.x;
+  if (t < prm.ntiles && threadIdx.x == 0) issue_tile<P, TE, KAHAN>(prm, t, stage0, bar0, &tm_u, &tm_cu, &tm_w, &tm_cw);
+  for (int it = 0; t < prm.ntiles; it++, t += gridDim.x) {
+    const int s = it & 1;
+    unsigned char *st = s ? stage1 : stage0;
+    const uint32_t bar = s ? bar1 : bar0;
+    const uint32_t parity = (it >> 1) & 1;
+    // prefetch the next tile into the other stage (freed by the barrier that ended the previous tile)
+    const int tn = t + gridDim.x;
+    if (threadIdx.x == 0 && tn < prm.ntiles) {
+      fence_proxy_async();
+      issue_tile<P, TE, KAHAN>(prm, tn, s ? stage0 : stage1, s ? bar0 : bar1, &tm_u, &tm_cu, &tm_w, &tm_cw);
+    }
+    const TileBox b = tile_box<P, TE>(prm, t);
+    const int xoff = b.EX0 * P - b.RXa;   // region-box column of the first region node
+    const bool active = (item < G::ITEMS) && (ecx < b.NEXa) && (ecy < b.NEYa);
+    const int ex = b.EX0 + ecx, ey = b.EY0 + ecy;
+    // per-element constants (global, L1/L2 resident) before the wait
+    float lam = 0.f, mu = 0.f, ix = 0.f, iy = 0.f, detJ = 0.f;
+    if (active) {
+      const size_t cell = (size_t)ey * prm.mx + ex;
+      lam = prm.lam[cell]; mu = prm.mu[cell];
+      ix = prm.iJ00[ex]; iy = prm.iJ11[ey];
+      detJ = prm.J00[ex] * prm.J11[ey];
+    }
+    const bool ok = mbar_wait_bounded(bar, parity);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        atomicExch(prm.err, 1);
+        // let this CTA's copies in flight land before the shared memory is released
+        mbar_wait_bounded(bar, parity);
+        if (tn < prm.ntiles) mbar_wait_bounded(s ? bar0 : bar1, ((it + 1) >> 1) & 1);
+      }
+      return;
+    }
+    const float2 *rU = reinterpret_cast<const float2 *>(st);
+    const float2 *rCU = reinterpret_cast<const float2 *>(st + L::REG);
+    const float2 *oW = reinterpret_cast<const float2 *>(st + (KAHAN ? 2 : 1) * L::REG);
+    const float2 *oCW = reinterpret_cast<const float2 *>(st + (KAHAN ? 2 : 1) * L::REG + L::OWN);
+
+    // ---- 1. derivatives along row j (registers) and column j (to X1) -----
+    float2 gxi[N1];
+    const int base = (ecy * P) * BXW + ecx * P + xoff;   // region-box index of element node (0,0)
+    if (active) {
+      {
+        const float2 u0 = rU[base + j * BXW];
+        const float2 c0 = KAHAN ? rCU[base + j * BXW] : make_float2(0.f, 0.f);
+        float2 d[N1];
+#pragma unroll
+        for (int k = 1; k < N1; k++) {
+          const float2 uk = rU[base + j * BXW + k];
+          d[k].x = uk.x - u0.x; d[k].y = uk.y - u0.y;
+          if (KAHAN) {
+            const float2 ck = rCU[base + j * BXW + k];
+            d[k].x -= (ck.x - c0.x); d[k].y -= (ck.y - c0.y);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < N1; q++) {
+          float sx = 0.f, sy = 0.f;
+#pragma unroll
+          for (int k = 1; k < N1; k++) { sx = fmaf(D[q * N1 + k], d[k].x, sx); sy = fmaf(D[q * N1 + k], d[k].y, sy); }
+          gxi[q] = make_float2(sx, sy);
+        }
+      }
+      {
+        const float2 u0 = rU[base + j];
+        const float2 c0 = KAHAN ? rCU[base + j] : make_float2(0.f, 0.f);
+        float2 d[N1];
+#pragma unroll
+        for (int k = 1; k < N1; k++) {
+          const float2 uk = rU[base + k * BXW + j];
+          d[k].x = uk.x - u0.x; d[k].y = uk.y - u0.y;
+          if (KAHAN) {
+            const float2 ck = rCU[base + k * BXW + j];
+            d[k].x -= (ck.x - c0.x); d[k].y -= (ck.y - c0.y);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < N1; q++) {
+          float sx = 0.f, sy = 0.f;
+#pragma unroll
+          for (int k = 1; k < N1; k++) { sx = fmaf(D[q * N1 + k], d[k].x, sx); sy = fmaf(D[q * N1 + k], d[k].y, sy); }
+          X1[el * NPE + j + q * N1] = make_float2(sx, sy);   // d/deta at (j, q)
+        }
+      }
+    }
+    __syncthreads();
+
+    // ---- 2. stress at the row's points; xi divergence; eta fluxes to X2 ---
+    float2 R[N1];
+    if (active) {
+      const float c11 = fmaf(2.f, mu, lam);
+      float2 Fxi[N1];
+#pragma unroll
+      for (int q = 0; q < N1; q++) {
+        const float2 ge = X1[el * NPE + q + j * N1];   // d/deta at (q, j)
+        const float e0 = ix * gxi[q].x, e1 = iy * ge.y, e2 = fmaf(ix, gxi[q].y, iy * ge.x);
+        const float nf = -(detJ * (W[q] * wj));
+        const float sxx = fmaf(c11, e0, lam * e1), syy = fmaf(lam, e0, c11 * e1), sxy = mu * e2;
+        Fxi[q] = make_float2(ix * nf * sxx, ix * nf * sxy);
+        X2[el * NPE + q + j * N1] = make_float2(iy * nf * sxy, iy * nf * syy);
+      }
+#pragma unroll
+      for (int a = 0; a < N1; a++) {
+        float rx = 0.f, ry = 0.f;
+#pragma unroll
+        for (int q = 0; q < N1; q++) { rx = fmaf(D[q * N1 + a], Fxi[q].x, rx); ry = fmaf(D[q * N1 + a], Fxi[q].y, ry); }
+        R[a] = make_float2(rx, ry);
+      }
+    }
+    __syncthreads();
+
+    // ---- 3. eta divergence for the row's nodes; element forces to X1 -----
+    if (active) {
+#pragma unroll
+      for (int a = 0; a < N1; a++) {
+        float cx = R[a].x, cy = R[a].y;
+#pragma unroll
+        for (int q = 0; q < N1; q++) {
+          const float2 f = X2[el * NPE + a + q * N1];
+          cx = fmaf(Dcj[q], f.x, cx); cy = fmaf(Dcj[q], f.y, cy);
+        }
+        X1[el * NPE + a + j * N1] = make_float2(cx, cy);
+      }
+    }
+    __syncthreads();
+
+    // ---- owned nodes: ordered element sum, sources, update ----------------
+    const int s0 = prm.tile_src_off[t], s1 = prm.tile_src_off[t + 1];
+    const int r0 = prm.tile_rec_off[t], r1 = prm.tile_rec_off[t + 1];
+    for (int o = threadIdx.x; o < OWM * OWM; o += NT) {
+      const int oy = o / OWM, ox = o - (o / OWM) * OWM;
+      if (ox >= b.OW || oy >= b.OH) continue;
+      const int X = b.X0 + ox, Y = b.Y0 + oy;
+      float fx = 0.f, fy = 0.f;
+      const int exB = X / P, eyB = Y / P;
+      const int exA = (X - exB * P == 0) ? exB - 1 : exB, eyA = (Y - eyB * P == 0) ? eyB - 1 : eyB;
+      for (int e_y = eyA; e_y <= eyB; e_y++) {
+        if (e_y < 0 || e_y >= prm.my) continue;
+        for (int e_x = exA; e_x <= exB; e_x++) {
+          if (e_x < 0 || e_x >= prm.mx) continue;
+          const float2 f = X1[((e_y - b.EY0) * NEX + (e_x - b.EX0)) * NPE + (X - e_x * P) + (Y - e_y * P) * N1];
+          fx += f.x; fy += f.y;
+        }
+      }
+      for (int q = s0; q < s1; q++) {
+        const int sidx = prm.tile_src_idx[q], se = prm.src_elem[sidx], sx = se % prm.mx, sy = se / prm.mx;
+        const int a = X - sx * P, bb = Y - sy * P;
+        if (a >= 0 && a <= P && bb >= 0 && bb <= P) {
+          const float val = (float)prm.stf[sidx];
+          const float *sv = prm.src_vals + (size_t)sidx * 2 * NPE + 2 * (a + bb * N1);
+          fx = fmaf(val, sv[0], fx); fy = fmaf(val, sv[1], fy);
+        }
+      }
+      const size_t n = (size_t)Y * prm.pitch + X;
+      const float minv = prm.minv[n];
+      const float2 acc = make_float2(fx * minv, fy * minv);
+      const int ri = (Y - b.RYa) * BXW + (X - b.RXa);
+      const int oi = oy * OBW + (X - b.OXa);
+      float2 u = rU[ri], w = oW[oi];
+      float2 cu = KAHAN ? rCU[ri] : make_float2(0.f, 0.f), cw = KAHAN ? oCW[oi] : make_float2(0.f, 0.f);
+      if (r1 > r0) {
+        const float2 v = make_float2(fmaf(prm.half_dt, acc.x, w.x), fmaf(prm.half_dt, acc.y, w.y));
+        for (int q = r0; q < r1; q++) {
+          const int r = prm.tile_rec_idx[q], re = prm.rec_elem[r], rx = re % prm.mx, ry = re / prm.mx;
+          const int a = X - rx * P, bb = Y - ry * P;
+          if (a >= 0 && a <= P && bb >= 0 && bb <= P) {
+            float *rb = prm.rbuf_out + ((size_t)r * NPE + a + bb * N1) * 6;
+            rb[0] = u.x; rb[1] = u.y; rb[2] = v.x; rb[3] = v.y; rb[4] = acc.x; rb[5] = acc.y;
+          }
+        }
+      }
+      if (KAHAN) {
+        kahan_add(w.x, cw.x, prm.dt * acc.x);
+        kahan_add(w.y, cw.y, prm.dt * acc.y);
+        kahan_add(u.x, cu.x, prm.dt * w.x);
+        kahan_add(u.y, cu.y, prm.dt * w.y);
+        prm.cu_out[n] = cu;
+        prm.cw_out[n] = cw;
+      } else {
+        w.x = fmaf(prm.dt, acc.x, w.x); w.y = fmaf(prm.dt, acc.y, w.y);
+        u.x = fmaf(prm.dt, w.x, u.x); u.y = fmaf(prm.dt, w.y, u.y);
+      }
+      prm.u_out[n] = u;
+      prm.w_out[n] = w;
+      if (prm.a_out) prm.a_out[n] = acc;
+    }
+    __syncthreads();   // stage s and the exchange buffers are free again
+  }
+}
+
+// receiver rows of the last step of a block
+template <int P>
+__global__ void persist_record(const Params prm)
+{
+  sample_rows<P>(prm);
+}
+
+}  // namespace se2p

@@ -1,0 +1,37 @@
+// se2gpu_persist_params.h -- launch parameters of the persistent FP32 step kernel.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace se2p {
+
+struct Params {
+  int mx, my, nx_g, ny_g, pitch;   // pitch: padded row length (nodes) of the device arrays
+  int ntx, nty, ntiles;
+  // outputs (padded layout, float2 per node)
+  float2 *u_out, *w_out, *cu_out, *cw_out;
+  float2 *a_out;                   // optional: a_k (last step of a block)
+  // inputs not loaded by TMA
+  const float *minv;               // padded, 1/M
+  const float *lam, *mu;           // per cell
+  const float *J00, *J11, *iJ00, *iJ11;
+  float dt, half_dt;
+  int nsrc;
+  const int *src_elem;
+  const float *src_vals;           // [nsrc][2*npe]
+  const double *stf;               // this step's values per source
+  // receivers
+  int nrec;
+  const int *rec_elem;
+  float *rbuf_out;                 // [nrec][npe][6] (u, v, a) of this step's receiver elements
+  const float *rbuf_in;            // previous step's, sampled into trace_row when record != 0
+  int record;
+  const int *rec_gll;
+  const double *Dd, *iJ00d, *iJ11d;
+  double *trace_row;
+  int *err;                        // error flag (bounded waits)
+  // per-tile lists (CSR over tiles) of the sources and receivers whose element
+  // touches the tile's owned nodes, built on the host
+  const int *tile_src_off, *tile_src_idx, *tile_rec_off, *tile_rec_idx;
+};
+
+}  // namespace se2p

@@ -251,11 +251,10 @@ int main(int argc, char **argv)
     printf("  [material]     mu = %1.8e\n", mu);
     printf("  [material]    rho = %1.8e\n", rho);
   }
-  for (s = 0; s < nsrc; s++)
-    printf("Moment: [ %+1.2e , %+1.2e ; %+1.2e , %+1.2e ]\n", src_m[4 * s], src_m[4 * s + 1], src_m[4 * s + 2], src_m[4 * s + 3]);
   if (se2_setup_create(&sp, &su)) { fprintf(stderr, "[se2wave_gpu] set-up error: %s\n", se2_host_last_error()); return 1; }
-  for (s = 0; s < nsrc; s++) {
+  for (s = 0; s < nsrc; s++) {  /* the demo prints each moment, then SeismicSourceCreate's lines (4626-4652) */
     int g = su->src_gll[s], e = su->src_elem[s], gi = g % su->n1, gj = g / su->n1;
+    printf("Moment: [ %+1.2e , %+1.2e ; %+1.2e , %+1.2e ]\n", src_m[4 * s], src_m[4 * s + 1], src_m[4 * s + 2], src_m[4 * s + 3]);
     printf("[SeismicSource] source (%+1.4e,%+1.4e) --> element %d | rank 0\n", src_xy[2 * s], src_xy[2 * s + 1], e);
     printf("[SeismicSource] source --> closest_gll %d xi: (%+1.4e,%+1.4e) [%d,%d] \n", g, su->xi[gi], su->xi[gj], gi, gj);
     printf("[SeismicSource] source --> closest_gll %d x:  (%+1.4e,%+1.4e)\n", g,
@@ -267,7 +266,7 @@ int main(int argc, char **argv)
 
   memset(&pr, 0, sizeof(pr));
   pr.mx = mx; pr.my = my; pr.p = p; pr.dt = su->dt;
-  pr.D = su->D; pr.wq = su->wq; pr.J00 = su->J00; pr.J11 = su->J11; pr.iJ00 = su->iJ00; pr.iJ11 = su->iJ11;
+  pr.D = su->D; pr.wq = su->wq; pr.w1d = su->w1d; pr.J00 = su->J00; pr.J11 = su->J11; pr.iJ00 = su->iJ00; pr.iJ11 = su->iJ11;
   pr.lambda = su->lambda; pr.mu = su->mu; pr.mass = su->mass;
   pr.nsrc = su->nsrc; pr.src_elem = su->src_elem; pr.src_vals = su->src_vals;
   pr.nrec = ignore_rec ? 0 : su->nrec; pr.rec_node = su->rec_node; pr.rec_elem = su->rec_elem; pr.rec_gll = su->rec_gll;

@@ -24,12 +24,12 @@ PRECISIONS = {"fp64": FP64, "fp32_kahan": FP32_KAHAN, "fp32": FP32}
 EXPORTS = ["se2gpu_create", "se2gpu_destroy", "se2gpu_last_error", "se2gpu_create_error", "se2gpu_set_stream",
            "se2gpu_synchronize", "se2gpu_set_fields", "se2gpu_get_fields", "se2gpu_advance", "se2gpu_traces",
            "se2gpu_norms", "se2gpu_assemble_linear_form", "se2gpu_assemble_linear_form_device", "se2gpu_info",
-           "se2gpu_device_fields"]
+           "se2gpu_device_fields", "se2gpu_tile_configs", "se2gpu_set_tile_config"]
 
 
 class _CProblem(C.Structure):
     _fields_ = [("mx", C.c_int), ("my", C.c_int), ("p", C.c_int), ("dt", C.c_double),
-                ("D", _dp), ("wq", _dp), ("J00", _dp), ("J11", _dp), ("iJ00", _dp), ("iJ11", _dp),
+                ("D", _dp), ("wq", _dp), ("w1d", _dp), ("J00", _dp), ("J11", _dp), ("iJ00", _dp), ("iJ11", _dp),
                 ("lambda_", _dp), ("mu", _dp), ("mass", _dp),
                 ("nsrc", C.c_int), ("src_elem", _ip), ("src_vals", _dp),
                 ("nrec", C.c_int), ("rec_node", _ip), ("rec_elem", _ip), ("rec_gll", _ip)]
@@ -66,6 +66,8 @@ def lib():
         L.se2gpu_assemble_linear_form_device.argtypes = [vp, vp, vp]
         L.se2gpu_info.argtypes = [vp, C.POINTER(C.c_long)]
         L.se2gpu_device_fields.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]
+        L.se2gpu_tile_configs.argtypes = [vp, _ip, _ip, C.c_int]
+        L.se2gpu_set_tile_config.argtypes = [vp, C.c_int]
         _lib = L
     return _lib
 
@@ -91,11 +93,11 @@ class Solver:
         self.setup = setup
         self.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
         s = setup
-        self._keep = [np.ascontiguousarray(x) for x in (s.D.reshape(-1), s.wq, s.J00, s.J11, s.iJ00, s.iJ11,
+        self._keep = [np.ascontiguousarray(x) for x in (s.D.reshape(-1), s.wq, s.w1d, s.J00, s.J11, s.iJ00, s.iJ11,
                                                        s.lam, s.mu, s.mass, s.src_elem, s.src_vals.reshape(-1),
                                                        s.rec_node, s.rec_elem, s.rec_gll)]
-        (D, wq, J00, J11, iJ00, iJ11, lam, mu, mass, se, sv, rn, re, rg) = self._keep
-        pr = _CProblem(mx=s.mx, my=s.my, p=s.p, dt=s.dt, D=_p(D), wq=_p(wq), J00=_p(J00), J11=_p(J11),
+        (D, wq, w1d, J00, J11, iJ00, iJ11, lam, mu, mass, se, sv, rn, re, rg) = self._keep
+        pr = _CProblem(mx=s.mx, my=s.my, p=s.p, dt=s.dt, D=_p(D), wq=_p(wq), w1d=_p(w1d), J00=_p(J00), J11=_p(J11),
                        iJ00=_p(iJ00), iJ11=_p(iJ11), lambda_=_p(lam), mu=_p(mu), mass=_p(mass),
                        nsrc=s.nsrc, src_elem=_p(se, _ip), src_vals=_p(sv),
                        nrec=s.nrec, rec_node=_p(rn, _ip), rec_elem=_p(re, _ip), rec_gll=_p(rg, _ip))
@@ -107,6 +109,7 @@ class Solver:
         if rc != 0:
             raise GpuError(f"se2gpu_create failed ({rc}): {lib().se2gpu_create_error().decode()}")
         self._h = h
+        self.tile_config = 0
         self.time = 0.0
         self.step = 0
         self._times = []
@@ -198,12 +201,23 @@ class Solver:
                     "se2gpu_assemble_linear_form_device")
 
     def info(self) -> dict:
-        a = (C.c_long * 8)()
+        a = (C.c_long * 9)()
         self._check(lib().se2gpu_info(self._h, a), "se2gpu_info")
-        keys = ["nx_g", "ny_g", "p", "precision", "nsrc", "nrec", "launches", "rows"]
+        keys = ["nx_g", "ny_g", "p", "precision", "nsrc", "nrec", "launches", "rows", "pitch"]
         return dict(zip(keys, list(a)))
 
     def device_fields(self):
         u, v, a = C.c_void_p(), C.c_void_p(), C.c_void_p()
         self._check(lib().se2gpu_device_fields(self._h, C.byref(u), C.byref(v), C.byref(a)), "se2gpu_device_fields")
         return u.value, v.value, a.value
+
+    def tile_configs(self):
+        """[(elements per tile edge, threads per CTA)] the step kernel offers for this problem."""
+        e = np.zeros(16, dtype=np.int32)
+        t = np.zeros(16, dtype=np.int32)
+        n = self._check(lib().se2gpu_tile_configs(self._h, _p(e, _ip), _p(t, _ip), 16), "se2gpu_tile_configs")
+        return [(int(e[i]), int(t[i])) for i in range(n)]
+
+    def set_tile_config(self, config: int):
+        self._check(lib().se2gpu_set_tile_config(self._h, int(config)), "se2gpu_set_tile_config")
+        self.tile_config = int(config)
