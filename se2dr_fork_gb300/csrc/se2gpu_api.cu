@@ -322,7 +322,7 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
     TRY(upload(h, &h->mass, P->mass, (size_t)nnodes));   // the reference divides by M
   } else {
     const bool kahan = (precision == SE2GPU_FP32_KAHAN);
-    h->pitch = (int)((nx_g + 15) / 16 * 16);
+    h->pitch = (int)((nx_g + 1 + 15) / 16 * 16);   // >= 1 padding node: paired reads stay in the row
     const size_t np = (size_t)ny_g * h->pitch;
     for (int b = 0; b < 2; b++) {
       TRY(dzero(h, (void **)&h->pu[b], np * 8));

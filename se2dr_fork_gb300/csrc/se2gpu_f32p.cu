@@ -84,7 +84,7 @@ int config_shape(int p, int config, bool kahan, TileShape *s)
   if (!e) return -1;
   s->tex = s->tey = e->te;
   s->nt = e->nt;
-  s->region_w = round_up((e->te + 1) * p + 2, 2);
+  s->region_w = round_up((e->te + 1) * p + 2 + ((p & 1) ? 2 : 0), 2);
   s->region_h = (e->te + 1) * p + 1;
   s->own_w = round_up(e->te * p + 2, 2);
   s->own_h = e->te * p + 1;

@@ -106,12 +106,15 @@ struct Geo {
   static constexpr int NEX = TE + 1, NE = NEX * NEX;      // elements incl. halo
   static constexpr int ITEMS = NE * N1;                   // (element, line) work items
   // region box (u, cu): the x start is rounded down to an even node so the copy
-  // starts on a 16-byte boundary; one extra column absorbs the shift
-  static constexpr int BXW = round_up(NEX * P + 2, 2);
+  // starts on a 16-byte boundary; one extra column absorbs the shift and two
+  // more keep the node phase's paired (16-byte) reads inside the box
+  static constexpr int BXW = round_up(NEX * P + 2 + ((P & 1) ? 2 : 0), 2);
   static constexpr int BXH = NEX * P + 1;
   static constexpr int OWM = TE * P + 1;                  // owned nodes per row (max)
   static constexpr int OBW = round_up(OWM + 1, 2);        // owned box (w, cw)
   static constexpr int OBH = OWM;
+  static constexpr int PW = OBW / 2;                      // node pairs per owned row
+  static constexpr int NPAIR = OWM * PW;
 };
 
 __host__ __device__ constexpr size_t al128(size_t x) { return (x + 127) & ~size_t(127); }
@@ -252,13 +255,27 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
     const int xoff = b.EX0 * P - b.RXa;   // region-box column of the first region node
     const bool active = (item < G::ITEMS) && (ecx < b.NEXa) && (ecy < b.NEYa);
     const int ex = b.EX0 + ecx, ey = b.EY0 + ecy;
-    // per-element constants (global, L1/L2 resident) before the wait
+    // global loads issued before the wait: per-element constants, the tile's
+    // source/receiver list bounds and 1/M of this thread's owned node pairs
     float lam = 0.f, mu = 0.f, ix = 0.f, iy = 0.f, detJ = 0.f;
     if (active) {
       const size_t cell = (size_t)ey * prm.mx + ex;
       lam = prm.lam[cell]; mu = prm.mu[cell];
       ix = prm.iJ00[ex]; iy = prm.iJ11[ey];
       detJ = prm.J00[ex] * prm.J11[ey];
+    }
+    const int s0 = prm.tile_src_off[t], s1 = prm.tile_src_off[t + 1];
+    const int r0 = prm.tile_rec_off[t], r1 = prm.tile_rec_off[t + 1];
+    constexpr int MAXP = (G::NPAIR + NT - 1) / NT;
+    float2 minv_pre[MAXP];
+#pragma unroll
+    for (int k = 0; k < MAXP; k++) {
+      const int o = threadIdx.x + k * NT;
+      const int oy = o / G::PW, px = o - (o / G::PW) * G::PW;
+      const int XA = b.OXa + 2 * px, Y = b.Y0 + oy;
+      minv_pre[k] = (o < G::NPAIR && oy < b.OH && XA < b.X0 + b.OW && XA + 1 >= b.X0)
+                        ? *reinterpret_cast<const float2 *>(prm.minv + (size_t)Y * prm.pitch + XA)
+                        : make_float2(0.f, 0.f);
     }
     const bool ok = mbar_wait_bounded(bar, parity);
     if (__syncthreads_or(!ok)) {
@@ -328,15 +345,17 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
     float2 R[N1];
     if (active) {
       const float c11 = fmaf(2.f, mu, lam);
+      const float nfj = -(detJ * wj);
       float2 Fxi[N1];
 #pragma unroll
       for (int q = 0; q < N1; q++) {
         const float2 ge = X1[el * NPE + q + j * N1];   // d/deta at (q, j)
         const float e0 = ix * gxi[q].x, e1 = iy * ge.y, e2 = fmaf(ix, gxi[q].y, iy * ge.x);
-        const float nf = -(detJ * (W[q] * wj));
+        const float nf = nfj * W[q];                   // -detJ w_q w_j
+        const float fx_ = ix * nf, fy_ = iy * nf;
         const float sxx = fmaf(c11, e0, lam * e1), syy = fmaf(lam, e0, c11 * e1), sxy = mu * e2;
-        Fxi[q] = make_float2(ix * nf * sxx, ix * nf * sxy);
-        X2[el * NPE + q + j * N1] = make_float2(iy * nf * sxy, iy * nf * syy);
+        Fxi[q] = make_float2(fx_ * sxx, fx_ * sxy);
+        X2[el * NPE + q + j * N1] = make_float2(fy_ * sxy, fy_ * syy);
       }
 #pragma unroll
       for (int a = 0; a < N1; a++) {
@@ -363,65 +382,94 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
     }
     __syncthreads();
 
-    // ---- owned nodes: ordered element sum, sources, update ----------------
-    const int s0 = prm.tile_src_off[t], s1 = prm.tile_src_off[t + 1];
-    const int r0 = prm.tile_rec_off[t], r1 = prm.tile_rec_off[t + 1];
-    for (int o = threadIdx.x; o < OWM * OWM; o += NT) {
-      const int oy = o / OWM, ox = o - (o / OWM) * OWM;
-      if (ox >= b.OW || oy >= b.OH) continue;
-      const int X = b.X0 + ox, Y = b.Y0 + oy;
-      float fx = 0.f, fy = 0.f;
-      const int exB = X / P, eyB = Y / P;
-      const int exA = (X - exB * P == 0) ? exB - 1 : exB, eyA = (Y - eyB * P == 0) ? eyB - 1 : eyB;
-      for (int e_y = eyA; e_y <= eyB; e_y++) {
-        if (e_y < 0 || e_y >= prm.my) continue;
-        for (int e_x = exA; e_x <= exB; e_x++) {
-          if (e_x < 0 || e_x >= prm.mx) continue;
-          const float2 f = X1[((e_y - b.EY0) * NEX + (e_x - b.EX0)) * NPE + (X - e_x * P) + (Y - e_y * P) * N1];
-          fx += f.x; fy += f.y;
+    // ---- owned nodes, two adjacent per thread: ordered element sum, sources, update
+#pragma unroll
+    for (int k = 0; k < MAXP; k++) {
+      const int o = threadIdx.x + k * NT;
+      if (o >= G::NPAIR) break;
+      const int oy = o / G::PW, px = o - (o / G::PW) * G::PW;
+      const int XA = b.OXa + 2 * px, Y = b.Y0 + oy;
+      const bool v0 = (oy < b.OH) && (XA >= b.X0) && (XA < b.X0 + b.OW);
+      const bool v1 = (oy < b.OH) && (XA + 1 >= b.X0) && (XA + 1 < b.X0 + b.OW);
+      if (!v0 && !v1) continue;
+      float f[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        if (!(h ? v1 : v0)) continue;
+        const int X = XA + h;
+        const int exB = X / P, eyB = Y / P;
+        const int exA = (X - exB * P == 0) ? exB - 1 : exB, eyA = (Y - eyB * P == 0) ? eyB - 1 : eyB;
+        for (int e_y = eyA; e_y <= eyB; e_y++) {
+          if (e_y < 0 || e_y >= prm.my) continue;
+          for (int e_x = exA; e_x <= exB; e_x++) {
+            if (e_x < 0 || e_x >= prm.mx) continue;
+            const float2 fe = X1[((e_y - b.EY0) * NEX + (e_x - b.EX0)) * NPE + (X - e_x * P) + (Y - e_y * P) * N1];
+            f[h][0] += fe.x; f[h][1] += fe.y;
+          }
         }
-      }
-      for (int q = s0; q < s1; q++) {
-        const int sidx = prm.tile_src_idx[q], se = prm.src_elem[sidx], sx = se % prm.mx, sy = se / prm.mx;
-        const int a = X - sx * P, bb = Y - sy * P;
-        if (a >= 0 && a <= P && bb >= 0 && bb <= P) {
-          const float val = (float)prm.stf[sidx];
-          const float *sv = prm.src_vals + (size_t)sidx * 2 * NPE + 2 * (a + bb * N1);
-          fx = fmaf(val, sv[0], fx); fy = fmaf(val, sv[1], fy);
-        }
-      }
-      const size_t n = (size_t)Y * prm.pitch + X;
-      const float minv = prm.minv[n];
-      const float2 acc = make_float2(fx * minv, fy * minv);
-      const int ri = (Y - b.RYa) * BXW + (X - b.RXa);
-      const int oi = oy * OBW + (X - b.OXa);
-      float2 u = rU[ri], w = oW[oi];
-      float2 cu = KAHAN ? rCU[ri] : make_float2(0.f, 0.f), cw = KAHAN ? oCW[oi] : make_float2(0.f, 0.f);
-      if (r1 > r0) {
-        const float2 v = make_float2(fmaf(prm.half_dt, acc.x, w.x), fmaf(prm.half_dt, acc.y, w.y));
-        for (int q = r0; q < r1; q++) {
-          const int r = prm.tile_rec_idx[q], re = prm.rec_elem[r], rx = re % prm.mx, ry = re / prm.mx;
-          const int a = X - rx * P, bb = Y - ry * P;
+        for (int q = s0; q < s1; q++) {
+          const int sidx = prm.tile_src_idx[q], se = prm.src_elem[sidx], sx = se % prm.mx, sy = se / prm.mx;
+          const int a = X - sx * P, bb = Y - sy * P;
           if (a >= 0 && a <= P && bb >= 0 && bb <= P) {
-            float *rb = prm.rbuf_out + ((size_t)r * NPE + a + bb * N1) * 6;
-            rb[0] = u.x; rb[1] = u.y; rb[2] = v.x; rb[3] = v.y; rb[4] = acc.x; rb[5] = acc.y;
+            const float val = (float)prm.stf[sidx];
+            const float *sv = prm.src_vals + (size_t)sidx * 2 * NPE + 2 * (a + bb * N1);
+            f[h][0] = fmaf(val, sv[0], f[h][0]); f[h][1] = fmaf(val, sv[1], f[h][1]);
+          }
+        }
+      }
+      const float4 acc = make_float4(f[0][0] * minv_pre[k].x, f[0][1] * minv_pre[k].x,
+                                     f[1][0] * minv_pre[k].y, f[1][1] * minv_pre[k].y);
+      const int ri = (Y - b.RYa) * BXW + (XA - b.RXa);     // even: 16-byte aligned pairs
+      const int oi = oy * OBW + (XA - b.OXa);
+      float4 u = *reinterpret_cast<const float4 *>(rU + ri);
+      float4 w = *reinterpret_cast<const float4 *>(oW + oi);
+      float4 cu = KAHAN ? *reinterpret_cast<const float4 *>(rCU + ri) : make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 cw = KAHAN ? *reinterpret_cast<const float4 *>(oCW + oi) : make_float4(0.f, 0.f, 0.f, 0.f);
+      if (r1 > r0) {
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          if (!(h ? v1 : v0)) continue;
+          const int X = XA + h;
+          const float ux = h ? u.z : u.x, uy = h ? u.w : u.y, wx = h ? w.z : w.x, wy = h ? w.w : w.y;
+          const float ax = h ? acc.z : acc.x, ay = h ? acc.w : acc.y;
+          for (int q = r0; q < r1; q++) {
+            const int r = prm.tile_rec_idx[q], re = prm.rec_elem[r], rx = re % prm.mx, ry = re / prm.mx;
+            const int a = X - rx * P, bb = Y - ry * P;
+            if (a >= 0 && a <= P && bb >= 0 && bb <= P) {
+              float *rb = prm.rbuf_out + ((size_t)r * NPE + a + bb * N1) * 6;
+              rb[0] = ux; rb[1] = uy; rb[2] = fmaf(prm.half_dt, ax, wx); rb[3] = fmaf(prm.half_dt, ay, wy);
+              rb[4] = ax; rb[5] = ay;
+            }
           }
         }
       }
       if (KAHAN) {
-        kahan_add(w.x, cw.x, prm.dt * acc.x);
-        kahan_add(w.y, cw.y, prm.dt * acc.y);
-        kahan_add(u.x, cu.x, prm.dt * w.x);
-        kahan_add(u.y, cu.y, prm.dt * w.y);
-        prm.cu_out[n] = cu;
-        prm.cw_out[n] = cw;
+        kahan_add(w.x, cw.x, prm.dt * acc.x); kahan_add(w.y, cw.y, prm.dt * acc.y);
+        kahan_add(w.z, cw.z, prm.dt * acc.z); kahan_add(w.w, cw.w, prm.dt * acc.w);
+        kahan_add(u.x, cu.x, prm.dt * w.x); kahan_add(u.y, cu.y, prm.dt * w.y);
+        kahan_add(u.z, cu.z, prm.dt * w.z); kahan_add(u.w, cu.w, prm.dt * w.w);
       } else {
         w.x = fmaf(prm.dt, acc.x, w.x); w.y = fmaf(prm.dt, acc.y, w.y);
+        w.z = fmaf(prm.dt, acc.z, w.z); w.w = fmaf(prm.dt, acc.w, w.w);
         u.x = fmaf(prm.dt, w.x, u.x); u.y = fmaf(prm.dt, w.y, u.y);
+        u.z = fmaf(prm.dt, w.z, u.z); u.w = fmaf(prm.dt, w.w, u.w);
       }
-      prm.u_out[n] = u;
-      prm.w_out[n] = w;
-      if (prm.a_out) prm.a_out[n] = acc;
+      const size_t n = (size_t)Y * prm.pitch + XA;
+      if (v0 && v1) {
+        *reinterpret_cast<float4 *>(prm.u_out + n) = u;
+        *reinterpret_cast<float4 *>(prm.w_out + n) = w;
+        if (KAHAN) { *reinterpret_cast<float4 *>(prm.cu_out + n) = cu; *reinterpret_cast<float4 *>(prm.cw_out + n) = cw; }
+        if (prm.a_out) *reinterpret_cast<float4 *>(prm.a_out + n) = acc;
+      } else {
+        const int h = v0 ? 0 : 1;
+        prm.u_out[n + h] = h ? make_float2(u.z, u.w) : make_float2(u.x, u.y);
+        prm.w_out[n + h] = h ? make_float2(w.z, w.w) : make_float2(w.x, w.y);
+        if (KAHAN) {
+          prm.cu_out[n + h] = h ? make_float2(cu.z, cu.w) : make_float2(cu.x, cu.y);
+          prm.cw_out[n + h] = h ? make_float2(cw.z, cw.w) : make_float2(cw.x, cw.y);
+        }
+        if (prm.a_out) prm.a_out[n + h] = h ? make_float2(acc.z, acc.w) : make_float2(acc.x, acc.y);
+      }
     }
     __syncthreads();   // stage s and the exchange buffers are free again
   }
