@@ -144,6 +144,21 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def replica_seconds(local_seconds: float, dist=None, device=None) -> float:
+    """Job time of N independent replicas: the slowest rank (max over ranks)."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return local_seconds
+    import torch
+    t = torch.tensor([local_seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(dof_per_replica: int, steps: int, world: int, seconds: float) -> float:
+    """Whole-job DOF-updates/s of `world` replicas of the same workload (weak scaling)."""
+    return world * dof_per_replica * steps / seconds
+
+
 def time_steps(sol, steps, warmup, stream, torch):
     """Device time of `steps` steps (CUDA events on the launching stream)."""
     sol.advance(warmup)
@@ -180,11 +195,7 @@ def run_ours(args, rank, world):
         torch.cuda.synchronize()
 
     def tmax(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return replica_seconds(x, dist, "cuda")
 
     spec = S.grf2048(args.mx, args.mx, p=4, nt=args.steps + args.warmup + 10)
     setup = H.Setup(spec)
@@ -215,7 +226,7 @@ def run_ours(args, rank, world):
         per = secs / k
         b = alg_bytes_per_node(prec, ne, nnodes)
         achieved = b * nnodes / per / 1e9
-        results[prec] = {"value": world * dof * k / secs, "ms_per_step": 1e3 * per, "steps": k, "tile": tile,
+        results[prec] = {"value": replica_value(dof, k, world, secs), "ms_per_step": 1e3 * per, "steps": k, "tile": tile,
                          "launches": launches, "clocks": clk.summary(),
                          "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                                       "frac": achieved / hbm, "traffic": None,
