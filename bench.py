@@ -291,6 +291,133 @@ def run_ours(args, rank, world):
         dist.destroy_process_group()
 
 
+def run_sweep(args):
+    """Degree sweep at ~16M nodes: mx = 4000, 2000, 1333, 1000, 800, 667, 571, 500 for p = 1..8
+    (GRF material as the 2048^2 workload, one JSON line per degree and precision)."""
+    import torch
+    from se2dr_fork_gb300 import autotune
+    from se2dr_fork_gb300 import gpu as G
+    from se2dr_fork_gb300 import host as H
+    from se2dr_fork_gb300 import spec as S
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    hbm, _ = peaks()
+    for p, mx in zip(range(1, 9), [4000, 2000, 1333, 1000, 800, 667, 571, 500]):
+        vp = H.gaussian_random_field(mx, mx, 5000.0, 0.1, 8.0, seed=2048)
+        sp = S.grf2048(mx, mx, p=p, nt=10 ** 6, cells=(vp, vp / 1.73, np.full_like(vp, 2700.0)))
+        sp = sp.replace(nearest_internal_gll=(p > 1))
+        setup = H.Setup(sp)
+        for prec in ["fp32_kahan", "fp64"]:
+            k = args.steps if prec != "fp64" else max(3, args.steps // 10)
+            if prec != "fp64" and args.autotune:
+                autotune.tune(setup, prec, steps=5)
+            sol = G.Solver(setup, prec, trace_capacity=k + args.warmup + 2)
+            if prec != "fp64":
+                autotune.apply(sol, prec)
+            sol.set_stream(stream.cuda_stream)
+            secs, launches = time_steps(sol, k, args.warmup, stream, torch)
+            tile = sol.tile_configs()[sol.tile_config] if prec != "fp64" else None
+            sol.close()
+            per = secs / k
+            b = alg_bytes_per_node(prec, setup.mx * setup.my, setup.nnodes)
+            print(json.dumps({"sweep": "degree", "p": p, "mx": mx, "nodes": setup.nnodes, "precision": prec,
+                              "dof_updates_per_s": 2 * setup.nnodes * k / secs, "ms_per_step": 1e3 * per,
+                              "hbm_frac": b * setup.nnodes / per / 1e9 / hbm, "tile": tile, "steps": k}), flush=True)
+        del setup
+
+
+def run_ensemble(args):
+    """Batched ensemble: `--shots` seeded shots (mx, my ~ U{32..512}, p in {3,4,6}, 2 layers +
+    elliptical inclusion, random source and moment tensor, Ricker f0 ~ U[5,20] Hz, 32 receivers,
+    5000 steps each), FP32 with Kahan-compensated updates, one persistent launch per degree group
+    per step, blocks of steps replayed as CUDA graphs.  Prints one JSON line."""
+    import concurrent.futures as cf
+    import torch
+    from se2dr_fork_gb300 import gpu as G
+    from se2dr_fork_gb300 import host as H
+    from se2dr_fork_gb300 import spec as S
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    specs = S.ensemble(args.shots, seed=3)
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        setups = list(ex.map(H.Setup, specs))
+    t_setup = time.perf_counter() - t0
+    prec = args.precision if args.precision != "fp64" else "fp32_kahan"
+    t0 = time.perf_counter()
+    ens = G.Ensemble(setups, prec, block=args.block)
+    t_create = time.perf_counter() - t0
+    stream = torch.cuda.Stream()
+    ens.set_stream(stream.cuda_stream)
+    nodes = sum(su.nnodes for su in setups)
+    ne = sum(su.mx * su.my for su in setups)
+    dof = 2 * nodes
+    hbm, peak_kind = peaks()
+    b = alg_bytes_per_node(prec, ne, nodes)
+
+    def timed(nsteps):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        ens.enqueue(nsteps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ens.synchronize()
+        return ev0.elapsed_time(ev1) / 1e3
+
+    tuned = {}
+    if args.autotune:
+        for p in ens.degrees():
+            times = []
+            for c in range(8):
+                try:
+                    ens.set_tile_config(p, c)
+                except G.GpuError:
+                    break
+                timed(args.block)
+                times.append(timed(args.block))
+            best = int(np.argmin(times))
+            ens.set_tile_config(p, best)
+            tuned[p] = {"config": best, "seconds": times}
+    ens.advance(args.block, traces=False)          # stage real STF values, build the graphs
+    timed(args.warmup * args.block)
+    launches0 = ens.info()["launches"]
+    with ClockSampler(0) as clk:
+        secs = timed(args.steps)
+    launches = ens.info()["launches"] - launches0
+    per = secs / args.steps
+    achieved = b * nodes / per / 1e9
+    # end to end through the C-ABI: host STF upload per block, receiver rows back to host memory
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    trs = ens.advance(args.steps)
+    e2e_s = time.perf_counter() - t0
+    nrec_total = sum(su.nrec for su in setups)
+    nsrc_total = sum(su.nsrc for su in setups)
+    steps_per_shot = 5000
+    line = {"metric": METRIC, "value": dof * args.steps / secs, "unit": "DOF/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup * args.block, "ms_per_step": 1e3 * per, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"ensemble: {args.shots} shots, mx, my ~ U{{32..512}}, p in {{3,4,6}}, 2 layers + "
+                                   f"elliptical inclusion, random moment tensor, Ricker f0 ~ U[5,20] Hz, 32 receivers",
+                       "precision": prec, "nodes": nodes, "dof": dof, "block": args.block,
+                       "degrees": {str(p): sum(1 for su in setups if su.p == p) for p in ens.degrees()},
+                       "tile_configs": {str(p): ens.tile_config(p) for p in ens.degrees()},
+                       "l2": "inputs larger than L2 (state %.1f GB)" % (nodes * 8 * (4 if prec == "fp32_kahan" else 2) / 1e9)},
+            "shots_per_s": args.shots * (args.steps / secs) / steps_per_shot,
+            "shot_steps": steps_per_shot,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": None, "alg_bytes_per_node": b, "peak_kind": peak_kind},
+            "clocks": clk.summary(), "gpu_launches": launches, "autotune": tuned or None,
+            "e2e": {"value": dof * args.steps / e2e_s, "unit": "DOF/s", "seconds": e2e_s,
+                    "shots_per_s": args.shots * (args.steps / e2e_s) / steps_per_shot,
+                    "h2d_bytes_per_step": 8 * nsrc_total, "d2h_bytes_per_step": 8 * 7 * nrec_total,
+                    "includes": "se2gpu_ensemble_advance: host STF upload per block, receiver rows to host memory"},
+            "setup_seconds": {"host": t_setup, "ensemble_create": t_create},
+            "trace_rows": int(sum(t.shape[0] for t in trs))}
+    ens.close()
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -305,12 +432,20 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=6)
     ap.add_argument("--tile-config", type=int, default=-1, help="step-kernel tile configuration (-1: autotuned or default)")
     ap.add_argument("--autotune", action="store_true", help="measure every tile configuration first and cache the best")
+    ap.add_argument("--sweep", action="store_true", help="degree sweep p = 1..8 at ~16M nodes instead of the headline run")
+    ap.add_argument("--ensemble", action="store_true", help="batched ensemble of --shots shots instead of the headline run")
+    ap.add_argument("--shots", type=int, default=256)
+    ap.add_argument("--block", type=int, default=100, help="ensemble steps per CUDA graph")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.sweep:
+        run_sweep(args)
+    elif args.ensemble and args.impl == "ours":
+        run_ensemble(args)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         run_ours(args, rank, world)

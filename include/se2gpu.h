@@ -120,6 +120,47 @@ int se2gpu_device_fields(const se2gpu_solver *h, void **u, void **v, void **a);
 int se2gpu_tile_configs(const se2gpu_solver *h, int *edge, int *threads, int max_configs);
 int se2gpu_set_tile_config(se2gpu_solver *h, int config);
 
+/* ---- Batched ensemble.  No counterpart in the reference, which runs one shot
+   per process (se2wave.c main): many independent problems ("shots") of any
+   mesh size and degree advanced in lock-step on one GPU, FP32 precisions only.
+   Each step is one persistent launch per degree present, over a flattened
+   (shot, tile) work list; each block of `block` steps is captured once as a
+   CUDA graph and replayed.  Every shot advances exactly as an se2gpu_solver of
+   the same problem and precision would (bit-identical fields and traces). */
+typedef struct se2gpu_ensemble se2gpu_ensemble;
+
+int  se2gpu_ensemble_create(const se2gpu_problem *shots, int nshots, int precision, int block, se2gpu_ensemble **out);
+void se2gpu_ensemble_destroy(se2gpu_ensemble *e);
+/* message of the handle's last failure; with NULL, of the last create failure in this thread */
+const char *se2gpu_ensemble_last_error(const se2gpu_ensemble *e);
+int se2gpu_ensemble_set_stream(se2gpu_ensemble *e, void *stream);
+/* graphs on (default) or plain launches */
+int se2gpu_ensemble_set_graphs(se2gpu_ensemble *e, int enable);
+/* tile configuration (se2gpu_tile_configs numbering) of all shots of degree p;
+   se2gpu_ensemble_tile_config returns the current one */
+int se2gpu_ensemble_set_tile_config(se2gpu_ensemble *e, int p, int config);
+int se2gpu_ensemble_tile_config(const se2gpu_ensemble *e, int p);
+
+/* Advance every shot nsteps steps.  Shot-major layouts, shot s's block at the
+   prefix sum of the earlier shots' counts:
+     stf    [shot][nsteps][nsrc_s]        source-time function values per step
+     traces [shot][nsteps][nrec_s][7]     receiver rows (ux uy vx vy ax ay curl(v)), FP64;
+                                          NULL = do not return them
+   Returns when the traces are in `traces`. */
+int se2gpu_ensemble_advance(se2gpu_ensemble *e, int nsteps, const double *stf, double *traces);
+/* Enqueue nsteps steps with the STF values already staged on the device and
+   without returning receiver rows; no synchronisation (device-resident timing). */
+int se2gpu_ensemble_enqueue(se2gpu_ensemble *e, int nsteps);
+int se2gpu_ensemble_synchronize(se2gpu_ensemble *e);
+
+/* One shot's fields as FP64 host arrays of 2*nnodes (as se2gpu_get/set_fields). */
+int se2gpu_ensemble_get_fields(se2gpu_ensemble *e, int shot, double *u, double *v, double *a);
+int se2gpu_ensemble_set_fields(se2gpu_ensemble *e, int shot, const double *u, const double *v, const double *a);
+
+/* ints[0..8] = shots, degree groups, block, kernel launches so far, graph
+   replays, total nodes, total sources, total receivers, (shot, tile) items. */
+int se2gpu_ensemble_info(const se2gpu_ensemble *e, long *ints);
+
 #ifdef __cplusplus
 }
 #endif

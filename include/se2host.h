@@ -101,6 +101,33 @@ int se2_stf_eval(int type, const double par[3], double time, double *value);
 int se2_gaussian_random_field(int mx, int my, double mean, double rel_std, double corr_cells,
                               unsigned long long seed, double *out);
 
+/* Seeded shot draws (splitmix64 stream per (seed, index)).  Kinds:
+   SE2_SHOT_ENSEMBLE  mx, my ~ U{32..512}, p in {3,4,6}, 32 receivers, 5000 steps,
+                      source anywhere in the central 80 %;
+   SE2_SHOT_TRAINING  128 x 128, p = 4, 16 surface receivers, 4096 steps, source in the lower half;
+   SE2_SHOT_OOD       as TRAINING with Vp up to 7500 m/s and two inclusions.
+   Elements are 31.25 m squares, the domain is [0, Lx] x [0, Ly].  Materials: two
+   layers split at interface_y plus elliptical inclusions, each rock with
+   Vp ~ U[3000, 6000] (7500 OOD), Vp/Vs ~ U[1.6, 1.9], rho ~ U[2000, 3000];
+   moment tensor entries Mxx, Mxy = Myx, Myy ~ N(0, 1e15); Ricker f0 ~ U[5, 20] Hz,
+   t0 = 1.5 / f0. */
+enum { SE2_SHOT_ENSEMBLE = 0, SE2_SHOT_TRAINING = 1, SE2_SHOT_OOD = 2 };
+typedef struct se2_shot_draw {
+  int mx, my, p, nrec;
+  long nsteps;
+  double h, Lx, Ly;
+  double interface_y;
+  double lower[3], upper[3];    /* (vp, vs, rho) below / above the interface */
+  int ninc;
+  double inc[2][8];             /* centre x, y, semi-axes a, b, rotation, vp, vs, rho */
+  double src_xy[2];
+  double moment[4];             /* Mxx, Mxy, Myx, Myy */
+  double f0, t0;
+} se2_shot_draw;
+int se2_shot_draw_params(unsigned long long seed, long index, int kind, se2_shot_draw *out);
+/* the drawn materials on the mx*my cell grid (row-major, x fastest), at cell centres */
+int se2_shot_materials(const se2_shot_draw *d, double *vp, double *vs, double *rho);
+
 #ifdef __cplusplus
 }
 #endif

@@ -301,6 +301,100 @@ int se2_gaussian_random_field(int mx, int my, double mean, double rel_std, doubl
 }
 
 /* ------------------------------------------------------------------ */
+/* shot draws: 2-layer + elliptical-inclusion materials, random source */
+/* ------------------------------------------------------------------ */
+static double unif(uint64_t *st, double a, double b)
+{
+  return a + (b - a) * ((double)(splitmix64(st) >> 11) * (1.0 / 9007199254740992.0));
+}
+
+static double normal(uint64_t *st)
+{
+  const double u1 = ((double)(splitmix64(st) >> 11) + 1.0) * (1.0 / 9007199254740992.0);
+  const double u2 = ((double)(splitmix64(st) >> 11)) * (1.0 / 9007199254740992.0);
+  return sqrt(-2.0 * log(u1)) * cos(2.0 * SE2_PI * u2);
+}
+
+static void draw_rock(uint64_t *st, double vp_max, double *v)
+{
+  v[0] = unif(st, 3000.0, vp_max);          /* Vp */
+  v[1] = v[0] / unif(st, 1.6, 1.9);         /* Vs from Vp/Vs */
+  v[2] = unif(st, 2000.0, 3000.0);          /* rho */
+}
+
+int se2_shot_draw_params(unsigned long long seed, long index, int kind, se2_shot_draw *d)
+{
+  uint64_t st = (uint64_t)seed * 0x9E3779B97F4A7C15ULL ^ ((uint64_t)index + 0x632BE59BD9B4E019ULL) * 0xD1B54A32D192ED03ULL;
+  const int degrees[3] = {3, 4, 6};
+  int i;
+  if (!d) SE2_FAIL("null output");
+  if (kind < 0 || kind > 2) SE2_FAIL("unknown shot kind %d", kind);
+  memset(d, 0, sizeof(*d));
+  splitmix64(&st);
+  if (kind == SE2_SHOT_ENSEMBLE) {
+    d->mx = 32 + (int)(splitmix64(&st) % 481);   /* U{32..512} */
+    d->my = 32 + (int)(splitmix64(&st) % 481);
+    d->p = degrees[splitmix64(&st) % 3];
+    d->nrec = 32;
+    d->nsteps = 5000;
+  } else {
+    d->mx = d->my = 128;
+    d->p = 4;
+    d->nrec = 16;
+    d->nsteps = 4096;
+  }
+  d->h = 31.25;                                  /* element size (m): 4 km / 128 */
+  d->Lx = d->mx * d->h;
+  d->Ly = d->my * d->h;
+  {
+    const double vp_max = (kind == SE2_SHOT_OOD) ? 7500.0 : 6000.0;
+    d->interface_y = unif(&st, 0.3, 0.7) * d->Ly;
+    draw_rock(&st, vp_max, d->lower);
+    draw_rock(&st, vp_max, d->upper);
+    d->ninc = (kind == SE2_SHOT_OOD) ? 2 : 1;
+    for (i = 0; i < d->ninc; i++) {
+      double *c = d->inc[i];
+      const double L = d->Lx < d->Ly ? d->Lx : d->Ly;
+      c[0] = unif(&st, 0.2, 0.8) * d->Lx;       /* centre */
+      c[1] = unif(&st, 0.2, 0.8) * d->Ly;
+      c[2] = unif(&st, 0.05, 0.2) * L;           /* semi-axes */
+      c[3] = unif(&st, 0.05, 0.2) * L;
+      c[4] = unif(&st, 0.0, SE2_PI);             /* rotation */
+      draw_rock(&st, vp_max, c + 5);
+    }
+  }
+  d->src_xy[0] = unif(&st, 0.1, 0.9) * d->Lx;
+  d->src_xy[1] = (kind == SE2_SHOT_ENSEMBLE) ? unif(&st, 0.1, 0.9) * d->Ly : unif(&st, 0.1, 0.5) * d->Ly;
+  d->moment[0] = 1.0e15 * normal(&st);           /* Mxx, Mxy, Myx, Myy: symmetric */
+  d->moment[1] = 1.0e15 * normal(&st);
+  d->moment[2] = d->moment[1];
+  d->moment[3] = 1.0e15 * normal(&st);
+  d->f0 = unif(&st, 5.0, 20.0);
+  d->t0 = 1.5 / d->f0;
+  return 0;
+}
+
+int se2_shot_materials(const se2_shot_draw *d, double *vp, double *vs, double *rho)
+{
+  int x, y, i;
+  if (!d || !vp || !vs || !rho) SE2_FAIL("null argument");
+  for (y = 0; y < d->my; y++)
+    for (x = 0; x < d->mx; x++) {
+      const double cx = (x + 0.5) * d->h, cy = (y + 0.5) * d->h;   /* cell centre */
+      const double *v = (cy < d->interface_y) ? d->lower : d->upper;
+      const long c = (long)y * d->mx + x;
+      for (i = 0; i < d->ninc; i++) {                               /* a later inclusion wins */
+        const double *e = d->inc[i];
+        const double dx = cx - e[0], dy = cy - e[1], cs = cos(e[4]), sn = sin(e[4]);
+        const double u = (cs * dx + sn * dy) / e[2], w = (-sn * dx + cs * dy) / e[3];
+        if (u * u + w * w <= 1.0) v = e + 5;
+      }
+      vp[c] = v[0]; vs[c] = v[1]; rho[c] = v[2];
+    }
+  return 0;
+}
+
+/* ------------------------------------------------------------------ */
 /* set-up                                                              */
 /* ------------------------------------------------------------------ */
 void se2_setup_destroy(se2_setup *s)

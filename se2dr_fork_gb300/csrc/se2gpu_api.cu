@@ -20,41 +20,10 @@
 #include <vector>
 
 #include "se2gpu.h"
+#include "se2gpu_internal.h"
 #include "se2gpu_launch.h"
 #include "se2gpu_persist_launch.h"
 
-struct se2gpu_solver {
-  int mx, my, p, n1, npe, nx_g, ny_g, precision;
-  long nnodes;
-  int nsrc, nrec, trace_cap, rows_written;
-  bool pending_record;
-  double dt;
-  int device, nsm;
-  cudaStream_t stream, own_stream;
-  size_t tsize;                  // compute precision (4 or 8 bytes)
-  // FP64 state: two buffer sets of packed u, v, a
-  void *f64[2][3];
-  int cur;
-  // FP32 leapfrog state (padded): u, w, cu, cw per buffer set, a of the last step
-  int pitch;
-  float2 *pu[2], *pw[2], *pcu[2], *pcw[2], *pa;
-  float *pminv, *rbuf[2];
-  int rlast;
-  CUtensorMap maps[2][4];
-  int pgrid, pconfig, pntx, pnty;
-  int *tile_src_off, *tile_src_idx, *tile_rec_off, *tile_rec_idx;
-  std::vector<int> *src_elem_h, *rec_elem_h;
-  int *err_dev;
-  // tables in compute precision
-  void *mass, *lam, *mu, *J00, *J11, *iJ00, *iJ11, *D, *wq, *src_vals;
-  double *Dd, *iJ00d, *iJ11d, *stf_dev, *traces, *norm_part;
-  int stf_cap;
-  int *src_elem, *rec_node, *rec_elem, *rec_gll;
-  void *scratch_u, *scratch_f;   // assemble_linear_form staging (packed)
-  long launches;
-  int ntx, nty, nblocks;         // FP64 tiles
-  char err[512];
-};
 
 static thread_local char g_create_err[512];
 
@@ -419,6 +388,8 @@ static se2p::Params f32_params(se2gpu_solver *h)
   prm.tile_rec_off = h->tile_rec_off; prm.tile_rec_idx = h->tile_rec_idx;
   return prm;
 }
+
+se2p::Params se2gpu_internal_f32_params(se2gpu_solver *h) { return f32_params(h); }
 
 // record the receivers of the last step if its row is still pending
 static int flush_record(se2gpu_solver *h)

@@ -23,7 +23,9 @@ cudaError_t set_tables(int p, const double *D, const double *w1d)
 struct Entry {
   int p, te, nt;
   size_t smem[2];                 // [kahan]
+  size_t bsmem[2];                // batched kernel [kahan]
   const void *fn[2];              // persist_step<...> [kahan]
+  const void *bfn[2];             // persist_batch<...> [kahan]
 };
 
 template <int P, int TE, int NT, bool K>
@@ -36,8 +38,12 @@ static Entry entry()
   e.p = P; e.te = TE; e.nt = NT;
   e.smem[0] = Layout<P, TE, false>::TOTAL;
   e.smem[1] = Layout<P, TE, true>::TOTAL;
+  e.bsmem[0] = Layout<P, TE, false>::BATCH_TOTAL;
+  e.bsmem[1] = Layout<P, TE, true>::BATCH_TOTAL;
   e.fn[0] = (const void *)persist_step<P, TE, NT, false>;
   e.fn[1] = (const void *)persist_step<P, TE, NT, true>;
+  e.bfn[0] = (const void *)persist_batch<P, TE, NT, false>;
+  e.bfn[1] = (const void *)persist_batch<P, TE, NT, true>;
   return e;
 }
 
@@ -96,17 +102,25 @@ cudaError_t prepare(int p, int config, bool kahan)
 {
   const Entry *e = find(p, config);
   if (!e) return cudaErrorInvalidValue;
-  const void *fn = e->fn[kahan ? 1 : 0];
-  cudaError_t r = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem[kahan ? 1 : 0]);
-  if (r != cudaSuccess) return r;
-  return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  const int k = kahan ? 1 : 0;
+  const void *fns[2] = {e->fn[k], e->bfn[k]};
+  const size_t sizes[2] = {e->smem[k], e->bsmem[k]};
+  for (int i = 0; i < 2; i++) {
+    const void *fn = fns[i];
+    cudaError_t r = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizes[i]);
+    if (r != cudaSuccess) return r;
+    r = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (r != cudaSuccess) return r;
+  }
+  return cudaSuccess;
 }
 
-int occupancy(int p, int config, bool kahan)
+int occupancy(int p, int config, bool kahan, bool batch)
 {
   const Entry *e = find(p, config);
   int n = 0;
-  if (!e || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, e->fn[kahan ? 1 : 0], e->nt, e->smem[kahan ? 1 : 0]) != cudaSuccess) {
+  if (!e || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, (batch ? e->bfn : e->fn)[kahan ? 1 : 0], e->nt,
+                                                          (batch ? e->bsmem : e->smem)[kahan ? 1 : 0]) != cudaSuccess) {
     cudaGetLastError();
     return 1;
   }
@@ -122,6 +136,33 @@ cudaError_t launch_step(int p, int config, bool kahan, const CUtensorMap *maps, 
   CUtensorMap m0 = maps[0], m1 = maps[1], m2 = maps[2], m3 = maps[3];
   void *args[] = {&m0, &m1, &m2, &m3, &pc};
   return cudaLaunchKernel(e->fn[kahan ? 1 : 0], dim3(grid), dim3(e->nt), args, e->smem[kahan ? 1 : 0], st);
+}
+
+cudaError_t launch_batch(int p, int config, bool kahan, const BatchArgs &ba, int grid, cudaStream_t st)
+{
+  const Entry *e = find(p, config);
+  if (!e) return cudaErrorInvalidValue;
+  BatchArgs a = ba;
+  void *args[] = {&a};
+  return cudaLaunchKernel(e->bfn[kahan ? 1 : 0], dim3(grid), dim3(e->nt), args, e->bsmem[kahan ? 1 : 0], st);
+}
+
+template <int P>
+static cudaError_t record_batch_t(const Params *shots, int nshots, int kblk, cudaStream_t st)
+{
+  persist_record_batch<P><<<nshots, 128, 0, st>>>(shots, nshots, kblk);
+  return cudaGetLastError();
+}
+cudaError_t launch_record_batch(int p, const Params *shots, int nshots, int kblk, cudaStream_t st)
+{
+  if (nshots <= 0) return cudaSuccess;
+  switch (p) {
+    case 1: return record_batch_t<1>(shots, nshots, kblk, st); case 2: return record_batch_t<2>(shots, nshots, kblk, st);
+    case 3: return record_batch_t<3>(shots, nshots, kblk, st); case 4: return record_batch_t<4>(shots, nshots, kblk, st);
+    case 5: return record_batch_t<5>(shots, nshots, kblk, st); case 6: return record_batch_t<6>(shots, nshots, kblk, st);
+    case 7: return record_batch_t<7>(shots, nshots, kblk, st); case 8: return record_batch_t<8>(shots, nshots, kblk, st);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 template <int P>

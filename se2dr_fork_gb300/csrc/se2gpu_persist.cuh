@@ -128,6 +128,8 @@ struct Layout {
   static constexpr size_t XCH = al128(sizeof(float2) * G::NE * G::NPE);   // exchange buffer
   static constexpr size_t MISC = 64;
   static constexpr size_t TOTAL = 2 * STAGE + 2 * XCH + MISC;
+  // the batched kernel keeps the current tile's shot parameters after the barriers
+  static constexpr size_t BATCH_TOTAL = TOTAL + al128(sizeof(Params));
   static constexpr uint32_t TX_BYTES =
       (uint32_t)((KAHAN ? 2 : 1) * (sizeof(float2) * G::BXW * G::BXH + sizeof(float2) * G::OBW * G::OBH));
 };
@@ -180,14 +182,14 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float inc)
 
 // receiver rows of the previous step from the side buffer (u, v, a per element node)
 template <int P>
-__device__ void sample_rows(const Params &prm)
+__device__ void sample_rows(const Params &prm, const float *rbuf_in, double *trace_row)
 {
   constexpr int N1 = P + 1, NPE = N1 * N1;
   for (int r = threadIdx.x; r < prm.nrec; r += blockDim.x) {
-    const float *rb = prm.rbuf_in + (size_t)r * NPE * 6;
+    const float *rb = rbuf_in + (size_t)r * NPE * 6;
     const int g = prm.rec_gll[r], eid = prm.rec_elem[r];
     const int ga = g % N1, gb = g / N1, ex = eid % prm.mx, ey = eid / prm.mx;
-    double *o = prm.trace_row + 7 * r;
+    double *o = trace_row + 7 * r;
     for (int c = 0; c < 6; c++) o[c] = (double)rb[g * 6 + c];
     const double ix = prm.iJ00d[ex], iy = prm.iJ11d[ey];
     double dvxdy = 0.0, dvydx = 0.0;
@@ -199,6 +201,234 @@ __device__ void sample_rows(const Params &prm)
   }
 }
 
+// one tile: prefetch of global values, wait for the tile's copies, the three
+// element phases and the node phase.  Returns false when the bounded wait expired.
+template <int P, int TE, int NT, bool KAHAN>
+__device__ __forceinline__ bool tile_body(const Params &prm, int t, const unsigned char *st, uint32_t bar,
+                                          uint32_t parity, float2 *X1, float2 *X2, int item, int el, int j, int ecx,
+                                          int ecy, const float (&Dcj)[P + 1], float wj)
+{
+  typedef Geo<P, TE> G;
+  typedef Layout<P, TE, KAHAN> L;
+  constexpr int N1 = G::N1, NPE = G::NPE, NEX = G::NEX, BXW = G::BXW, OBW = G::OBW;
+  const float *D = c_D[P - 1];
+  const float *W = c_w[P - 1];
+  const TileBox b = tile_box<P, TE>(prm, t);
+  const int xoff = b.EX0 * P - b.RXa;   // region-box column of the first region node
+  const bool active = (item < G::ITEMS) && (ecx < b.NEXa) && (ecy < b.NEYa);
+  const int ex = b.EX0 + ecx, ey = b.EY0 + ecy;
+  // global loads issued before the wait: per-element constants, the tile's
+  // source/receiver list bounds and 1/M of this thread's owned node pairs
+  float lam = 0.f, mu = 0.f, ix = 0.f, iy = 0.f, detJ = 0.f;
+  if (active) {
+    const size_t cell = (size_t)ey * prm.mx + ex;
+    lam = prm.lam[cell]; mu = prm.mu[cell];
+    ix = prm.iJ00[ex]; iy = prm.iJ11[ey];
+    detJ = prm.J00[ex] * prm.J11[ey];
+  }
+  const int s0 = prm.tile_src_off[t], s1 = prm.tile_src_off[t + 1];
+  const int r0 = prm.tile_rec_off[t], r1 = prm.tile_rec_off[t + 1];
+  constexpr int MAXP = (G::NPAIR + NT - 1) / NT;
+  float2 minv_pre[MAXP];
+#pragma unroll
+  for (int k = 0; k < MAXP; k++) {
+    const int o = threadIdx.x + k * NT;
+    const int oy = o / G::PW, px = o - (o / G::PW) * G::PW;
+    const int XA = b.OXa + 2 * px, Y = b.Y0 + oy;
+    minv_pre[k] = (o < G::NPAIR && oy < b.OH && XA < b.X0 + b.OW && XA + 1 >= b.X0)
+                      ? *reinterpret_cast<const float2 *>(prm.minv + (size_t)Y * prm.pitch + XA)
+                      : make_float2(0.f, 0.f);
+  }
+  const bool ok = mbar_wait_bounded(bar, parity);
+  if (__syncthreads_or(!ok)) return false;
+  const float2 *rU = reinterpret_cast<const float2 *>(st);
+  const float2 *rCU = reinterpret_cast<const float2 *>(st + L::REG);
+  const float2 *oW = reinterpret_cast<const float2 *>(st + (KAHAN ? 2 : 1) * L::REG);
+  const float2 *oCW = reinterpret_cast<const float2 *>(st + (KAHAN ? 2 : 1) * L::REG + L::OWN);
+
+  // ---- 1. derivatives along row j (registers) and column j (to X1) -----
+  float2 gxi[N1];
+  const int base = (ecy * P) * BXW + ecx * P + xoff;   // region-box index of element node (0,0)
+  if (active) {
+    {
+      const float2 u0 = rU[base + j * BXW];
+      const float2 c0 = KAHAN ? rCU[base + j * BXW] : make_float2(0.f, 0.f);
+      float2 d[N1];
+#pragma unroll
+      for (int k = 1; k < N1; k++) {
+        const float2 uk = rU[base + j * BXW + k];
+        d[k].x = uk.x - u0.x; d[k].y = uk.y - u0.y;
+        if (KAHAN) {
+          const float2 ck = rCU[base + j * BXW + k];
+          d[k].x -= (ck.x - c0.x); d[k].y -= (ck.y - c0.y);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < N1; q++) {
+        float sx = 0.f, sy = 0.f;
+#pragma unroll
+        for (int k = 1; k < N1; k++) { sx = fmaf(D[q * N1 + k], d[k].x, sx); sy = fmaf(D[q * N1 + k], d[k].y, sy); }
+        gxi[q] = make_float2(sx, sy);
+      }
+    }
+    {
+      const float2 u0 = rU[base + j];
+      const float2 c0 = KAHAN ? rCU[base + j] : make_float2(0.f, 0.f);
+      float2 d[N1];
+#pragma unroll
+      for (int k = 1; k < N1; k++) {
+        const float2 uk = rU[base + k * BXW + j];
+        d[k].x = uk.x - u0.x; d[k].y = uk.y - u0.y;
+        if (KAHAN) {
+          const float2 ck = rCU[base + k * BXW + j];
+          d[k].x -= (ck.x - c0.x); d[k].y -= (ck.y - c0.y);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < N1; q++) {
+        float sx = 0.f, sy = 0.f;
+#pragma unroll
+        for (int k = 1; k < N1; k++) { sx = fmaf(D[q * N1 + k], d[k].x, sx); sy = fmaf(D[q * N1 + k], d[k].y, sy); }
+        X1[el * NPE + j + q * N1] = make_float2(sx, sy);   // d/deta at (j, q)
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- 2. stress at the row's points; xi divergence; eta fluxes to X2 ---
+  float2 R[N1];
+  if (active) {
+    const float c11 = fmaf(2.f, mu, lam);
+    const float nfj = -(detJ * wj);
+    float2 Fxi[N1];
+#pragma unroll
+    for (int q = 0; q < N1; q++) {
+      const float2 ge = X1[el * NPE + q + j * N1];   // d/deta at (q, j)
+      const float e0 = ix * gxi[q].x, e1 = iy * ge.y, e2 = fmaf(ix, gxi[q].y, iy * ge.x);
+      const float nf = nfj * W[q];                   // -detJ w_q w_j
+      const float fx_ = ix * nf, fy_ = iy * nf;
+      const float sxx = fmaf(c11, e0, lam * e1), syy = fmaf(lam, e0, c11 * e1), sxy = mu * e2;
+      Fxi[q] = make_float2(fx_ * sxx, fx_ * sxy);
+      X2[el * NPE + q + j * N1] = make_float2(fy_ * sxy, fy_ * syy);
+    }
+#pragma unroll
+    for (int a = 0; a < N1; a++) {
+      float rx = 0.f, ry = 0.f;
+#pragma unroll
+      for (int q = 0; q < N1; q++) { rx = fmaf(D[q * N1 + a], Fxi[q].x, rx); ry = fmaf(D[q * N1 + a], Fxi[q].y, ry); }
+      R[a] = make_float2(rx, ry);
+    }
+  }
+  __syncthreads();
+
+  // ---- 3. eta divergence for the row's nodes; element forces to X1 -----
+  if (active) {
+#pragma unroll
+    for (int a = 0; a < N1; a++) {
+      float cx = R[a].x, cy = R[a].y;
+#pragma unroll
+      for (int q = 0; q < N1; q++) {
+        const float2 f = X2[el * NPE + a + q * N1];
+        cx = fmaf(Dcj[q], f.x, cx); cy = fmaf(Dcj[q], f.y, cy);
+      }
+      X1[el * NPE + a + j * N1] = make_float2(cx, cy);
+    }
+  }
+  __syncthreads();
+
+  // ---- owned nodes, two adjacent per thread: ordered element sum, sources, update
+#pragma unroll
+  for (int k = 0; k < MAXP; k++) {
+    const int o = threadIdx.x + k * NT;
+    if (o >= G::NPAIR) break;
+    const int oy = o / G::PW, px = o - (o / G::PW) * G::PW;
+    const int XA = b.OXa + 2 * px, Y = b.Y0 + oy;
+    const bool v0 = (oy < b.OH) && (XA >= b.X0) && (XA < b.X0 + b.OW);
+    const bool v1 = (oy < b.OH) && (XA + 1 >= b.X0) && (XA + 1 < b.X0 + b.OW);
+    if (!v0 && !v1) continue;
+    float f[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      if (!(h ? v1 : v0)) continue;
+      const int X = XA + h;
+      const int exB = X / P, eyB = Y / P;
+      const int exA = (X - exB * P == 0) ? exB - 1 : exB, eyA = (Y - eyB * P == 0) ? eyB - 1 : eyB;
+      for (int e_y = eyA; e_y <= eyB; e_y++) {
+        if (e_y < 0 || e_y >= prm.my) continue;
+        for (int e_x = exA; e_x <= exB; e_x++) {
+          if (e_x < 0 || e_x >= prm.mx) continue;
+          const float2 fe = X1[((e_y - b.EY0) * NEX + (e_x - b.EX0)) * NPE + (X - e_x * P) + (Y - e_y * P) * N1];
+          f[h][0] += fe.x; f[h][1] += fe.y;
+        }
+      }
+      for (int q = s0; q < s1; q++) {
+        const int sidx = prm.tile_src_idx[q], se = prm.src_elem[sidx], sx = se % prm.mx, sy = se / prm.mx;
+        const int a = X - sx * P, bb = Y - sy * P;
+        if (a >= 0 && a <= P && bb >= 0 && bb <= P) {
+          const float val = (float)prm.stf[sidx];
+          const float *sv = prm.src_vals + (size_t)sidx * 2 * NPE + 2 * (a + bb * N1);
+          f[h][0] = fmaf(val, sv[0], f[h][0]); f[h][1] = fmaf(val, sv[1], f[h][1]);
+        }
+      }
+    }
+    const float4 acc = make_float4(f[0][0] * minv_pre[k].x, f[0][1] * minv_pre[k].x,
+                                   f[1][0] * minv_pre[k].y, f[1][1] * minv_pre[k].y);
+    const int ri = (Y - b.RYa) * BXW + (XA - b.RXa);     // even: 16-byte aligned pairs
+    const int oi = oy * OBW + (XA - b.OXa);
+    float4 u = *reinterpret_cast<const float4 *>(rU + ri);
+    float4 w = *reinterpret_cast<const float4 *>(oW + oi);
+    float4 cu = KAHAN ? *reinterpret_cast<const float4 *>(rCU + ri) : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 cw = KAHAN ? *reinterpret_cast<const float4 *>(oCW + oi) : make_float4(0.f, 0.f, 0.f, 0.f);
+    if (r1 > r0) {
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        if (!(h ? v1 : v0)) continue;
+        const int X = XA + h;
+        const float ux = h ? u.z : u.x, uy = h ? u.w : u.y, wx = h ? w.z : w.x, wy = h ? w.w : w.y;
+        const float ax = h ? acc.z : acc.x, ay = h ? acc.w : acc.y;
+        for (int q = r0; q < r1; q++) {
+          const int r = prm.tile_rec_idx[q], re = prm.rec_elem[r], rx = re % prm.mx, ry = re / prm.mx;
+          const int a = X - rx * P, bb = Y - ry * P;
+          if (a >= 0 && a <= P && bb >= 0 && bb <= P) {
+            float *rb = prm.rbuf_out + ((size_t)r * NPE + a + bb * N1) * 6;
+            rb[0] = ux; rb[1] = uy; rb[2] = fmaf(prm.half_dt, ax, wx); rb[3] = fmaf(prm.half_dt, ay, wy);
+            rb[4] = ax; rb[5] = ay;
+          }
+        }
+      }
+    }
+    if (KAHAN) {
+      kahan_add(w.x, cw.x, prm.dt * acc.x); kahan_add(w.y, cw.y, prm.dt * acc.y);
+      kahan_add(w.z, cw.z, prm.dt * acc.z); kahan_add(w.w, cw.w, prm.dt * acc.w);
+      kahan_add(u.x, cu.x, prm.dt * w.x); kahan_add(u.y, cu.y, prm.dt * w.y);
+      kahan_add(u.z, cu.z, prm.dt * w.z); kahan_add(u.w, cu.w, prm.dt * w.w);
+    } else {
+      w.x = fmaf(prm.dt, acc.x, w.x); w.y = fmaf(prm.dt, acc.y, w.y);
+      w.z = fmaf(prm.dt, acc.z, w.z); w.w = fmaf(prm.dt, acc.w, w.w);
+      u.x = fmaf(prm.dt, w.x, u.x); u.y = fmaf(prm.dt, w.y, u.y);
+      u.z = fmaf(prm.dt, w.z, u.z); u.w = fmaf(prm.dt, w.w, u.w);
+    }
+    const size_t n = (size_t)Y * prm.pitch + XA;
+    if (v0 && v1) {
+      *reinterpret_cast<float4 *>(prm.u_out + n) = u;
+      *reinterpret_cast<float4 *>(prm.w_out + n) = w;
+      if (KAHAN) { *reinterpret_cast<float4 *>(prm.cu_out + n) = cu; *reinterpret_cast<float4 *>(prm.cw_out + n) = cw; }
+      if (prm.a_out) *reinterpret_cast<float4 *>(prm.a_out + n) = acc;
+    } else {
+      const int h = v0 ? 0 : 1;
+      prm.u_out[n + h] = h ? make_float2(u.z, u.w) : make_float2(u.x, u.y);
+      prm.w_out[n + h] = h ? make_float2(w.z, w.w) : make_float2(w.x, w.y);
+      if (KAHAN) {
+        prm.cu_out[n + h] = h ? make_float2(cu.z, cu.w) : make_float2(cu.x, cu.y);
+        prm.cw_out[n + h] = h ? make_float2(cw.z, cw.w) : make_float2(cw.x, cw.y);
+      }
+      if (prm.a_out) prm.a_out[n + h] = h ? make_float2(acc.z, acc.w) : make_float2(acc.x, acc.y);
+    }
+  }
+  __syncthreads();   // stage s and the exchange buffers are free again
+  return true;
+}
+
 template <int P, int TE, int NT, bool KAHAN>
 __global__ void __launch_bounds__(NT, ((2 * (Layout<P, TE, KAHAN>::TOTAL + 1024) <= 233472) ? 2 : 1))
 persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ CUtensorMap tm_cu,
@@ -207,7 +437,7 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
 {
   typedef Geo<P, TE> G;
   typedef Layout<P, TE, KAHAN> L;
-  constexpr int N1 = G::N1, NPE = G::NPE, NEX = G::NEX, BXW = G::BXW, OBW = G::OBW, OWM = G::OWM;
+  constexpr int N1 = G::N1, NEX = G::NEX;
   static_assert(NT >= G::ITEMS, "one (element, line) item per thread");
   const float *D = c_D[P - 1];
   const float *W = c_w[P - 1];
@@ -227,7 +457,7 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
     if (KAHAN) { prefetch_map(&tm_cu); prefetch_map(&tm_cw); }
   }
   __syncthreads();
-  if (blockIdx.x == 0 && prm.record) sample_rows<P>(prm);
+  if (blockIdx.x == 0 && prm.record) sample_rows<P>(prm, prm.rbuf_in, prm.trace_row);
 
   // this thread's (element, line) item, the same for every tile
   const int item = threadIdx.x;
@@ -242,7 +472,6 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
   if (t < prm.ntiles && threadIdx.x == 0) issue_tile<P, TE, KAHAN>(prm, t, stage0, bar0, &tm_u, &tm_cu, &tm_w, &tm_cw);
   for (int it = 0; t < prm.ntiles; it++, t += gridDim.x) {
     const int s = it & 1;
-    unsigned char *st = s ? stage1 : stage0;
     const uint32_t bar = s ? bar1 : bar0;
     const uint32_t parity = (it >> 1) & 1;
     // prefetch the next tile into the other stage (freed by the barrier that ended the previous tile)
@@ -251,34 +480,7 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
       fence_proxy_async();
       issue_tile<P, TE, KAHAN>(prm, tn, s ? stage0 : stage1, s ? bar0 : bar1, &tm_u, &tm_cu, &tm_w, &tm_cw);
     }
-    const TileBox b = tile_box<P, TE>(prm, t);
-    const int xoff = b.EX0 * P - b.RXa;   // region-box column of the first region node
-    const bool active = (item < G::ITEMS) && (ecx < b.NEXa) && (ecy < b.NEYa);
-    const int ex = b.EX0 + ecx, ey = b.EY0 + ecy;
-    // global loads issued before the wait: per-element constants, the tile's
-    // source/receiver list bounds and 1/M of this thread's owned node pairs
-    float lam = 0.f, mu = 0.f, ix = 0.f, iy = 0.f, detJ = 0.f;
-    if (active) {
-      const size_t cell = (size_t)ey * prm.mx + ex;
-      lam = prm.lam[cell]; mu = prm.mu[cell];
-      ix = prm.iJ00[ex]; iy = prm.iJ11[ey];
-      detJ = prm.J00[ex] * prm.J11[ey];
-    }
-    const int s0 = prm.tile_src_off[t], s1 = prm.tile_src_off[t + 1];
-    const int r0 = prm.tile_rec_off[t], r1 = prm.tile_rec_off[t + 1];
-    constexpr int MAXP = (G::NPAIR + NT - 1) / NT;
-    float2 minv_pre[MAXP];
-#pragma unroll
-    for (int k = 0; k < MAXP; k++) {
-      const int o = threadIdx.x + k * NT;
-      const int oy = o / G::PW, px = o - (o / G::PW) * G::PW;
-      const int XA = b.OXa + 2 * px, Y = b.Y0 + oy;
-      minv_pre[k] = (o < G::NPAIR && oy < b.OH && XA < b.X0 + b.OW && XA + 1 >= b.X0)
-                        ? *reinterpret_cast<const float2 *>(prm.minv + (size_t)Y * prm.pitch + XA)
-                        : make_float2(0.f, 0.f);
-    }
-    const bool ok = mbar_wait_bounded(bar, parity);
-    if (__syncthreads_or(!ok)) {
+    if (!tile_body<P, TE, NT, KAHAN>(prm, t, s ? stage1 : stage0, bar, parity, X1, X2, item, el, j, ecx, ecy, Dcj, wj)) {
       if (threadIdx.x == 0) {
         atomicExch(prm.err, 1);
         // let this CTA's copies in flight land before the shared memory is released
@@ -287,199 +489,120 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
       }
       return;
     }
-    const float2 *rU = reinterpret_cast<const float2 *>(st);
-    const float2 *rCU = reinterpret_cast<const float2 *>(st + L::REG);
-    const float2 *oW = reinterpret_cast<const float2 *>(st + (KAHAN ? 2 : 1) * L::REG);
-    const float2 *oCW = reinterpret_cast<const float2 *>(st + (KAHAN ? 2 : 1) * L::REG + L::OWN);
-
-    // ---- 1. derivatives along row j (registers) and column j (to X1) -----
-    float2 gxi[N1];
-    const int base = (ecy * P) * BXW + ecx * P + xoff;   // region-box index of element node (0,0)
-    if (active) {
-      {
-        const float2 u0 = rU[base + j * BXW];
-        const float2 c0 = KAHAN ? rCU[base + j * BXW] : make_float2(0.f, 0.f);
-        float2 d[N1];
-#pragma unroll
-        for (int k = 1; k < N1; k++) {
-          const float2 uk = rU[base + j * BXW + k];
-          d[k].x = uk.x - u0.x; d[k].y = uk.y - u0.y;
-          if (KAHAN) {
-            const float2 ck = rCU[base + j * BXW + k];
-            d[k].x -= (ck.x - c0.x); d[k].y -= (ck.y - c0.y);
-          }
-        }
-#pragma unroll
-        for (int q = 0; q < N1; q++) {
-          float sx = 0.f, sy = 0.f;
-#pragma unroll
-          for (int k = 1; k < N1; k++) { sx = fmaf(D[q * N1 + k], d[k].x, sx); sy = fmaf(D[q * N1 + k], d[k].y, sy); }
-          gxi[q] = make_float2(sx, sy);
-        }
-      }
-      {
-        const float2 u0 = rU[base + j];
-        const float2 c0 = KAHAN ? rCU[base + j] : make_float2(0.f, 0.f);
-        float2 d[N1];
-#pragma unroll
-        for (int k = 1; k < N1; k++) {
-          const float2 uk = rU[base + k * BXW + j];
-          d[k].x = uk.x - u0.x; d[k].y = uk.y - u0.y;
-          if (KAHAN) {
-            const float2 ck = rCU[base + k * BXW + j];
-            d[k].x -= (ck.x - c0.x); d[k].y -= (ck.y - c0.y);
-          }
-        }
-#pragma unroll
-        for (int q = 0; q < N1; q++) {
-          float sx = 0.f, sy = 0.f;
-#pragma unroll
-          for (int k = 1; k < N1; k++) { sx = fmaf(D[q * N1 + k], d[k].x, sx); sy = fmaf(D[q * N1 + k], d[k].y, sy); }
-          X1[el * NPE + j + q * N1] = make_float2(sx, sy);   // d/deta at (j, q)
-        }
-      }
-    }
-    __syncthreads();
-
-    // ---- 2. stress at the row's points; xi divergence; eta fluxes to X2 ---
-    float2 R[N1];
-    if (active) {
-      const float c11 = fmaf(2.f, mu, lam);
-      const float nfj = -(detJ * wj);
-      float2 Fxi[N1];
-#pragma unroll
-      for (int q = 0; q < N1; q++) {
-        const float2 ge = X1[el * NPE + q + j * N1];   // d/deta at (q, j)
-        const float e0 = ix * gxi[q].x, e1 = iy * ge.y, e2 = fmaf(ix, gxi[q].y, iy * ge.x);
-        const float nf = nfj * W[q];                   // -detJ w_q w_j
-        const float fx_ = ix * nf, fy_ = iy * nf;
-        const float sxx = fmaf(c11, e0, lam * e1), syy = fmaf(lam, e0, c11 * e1), sxy = mu * e2;
-        Fxi[q] = make_float2(fx_ * sxx, fx_ * sxy);
-        X2[el * NPE + q + j * N1] = make_float2(fy_ * sxy, fy_ * syy);
-      }
-#pragma unroll
-      for (int a = 0; a < N1; a++) {
-        float rx = 0.f, ry = 0.f;
-#pragma unroll
-        for (int q = 0; q < N1; q++) { rx = fmaf(D[q * N1 + a], Fxi[q].x, rx); ry = fmaf(D[q * N1 + a], Fxi[q].y, ry); }
-        R[a] = make_float2(rx, ry);
-      }
-    }
-    __syncthreads();
-
-    // ---- 3. eta divergence for the row's nodes; element forces to X1 -----
-    if (active) {
-#pragma unroll
-      for (int a = 0; a < N1; a++) {
-        float cx = R[a].x, cy = R[a].y;
-#pragma unroll
-        for (int q = 0; q < N1; q++) {
-          const float2 f = X2[el * NPE + a + q * N1];
-          cx = fmaf(Dcj[q], f.x, cx); cy = fmaf(Dcj[q], f.y, cy);
-        }
-        X1[el * NPE + a + j * N1] = make_float2(cx, cy);
-      }
-    }
-    __syncthreads();
-
-    // ---- owned nodes, two adjacent per thread: ordered element sum, sources, update
-#pragma unroll
-    for (int k = 0; k < MAXP; k++) {
-      const int o = threadIdx.x + k * NT;
-      if (o >= G::NPAIR) break;
-      const int oy = o / G::PW, px = o - (o / G::PW) * G::PW;
-      const int XA = b.OXa + 2 * px, Y = b.Y0 + oy;
-      const bool v0 = (oy < b.OH) && (XA >= b.X0) && (XA < b.X0 + b.OW);
-      const bool v1 = (oy < b.OH) && (XA + 1 >= b.X0) && (XA + 1 < b.X0 + b.OW);
-      if (!v0 && !v1) continue;
-      float f[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        if (!(h ? v1 : v0)) continue;
-        const int X = XA + h;
-        const int exB = X / P, eyB = Y / P;
-        const int exA = (X - exB * P == 0) ? exB - 1 : exB, eyA = (Y - eyB * P == 0) ? eyB - 1 : eyB;
-        for (int e_y = eyA; e_y <= eyB; e_y++) {
-          if (e_y < 0 || e_y >= prm.my) continue;
-          for (int e_x = exA; e_x <= exB; e_x++) {
-            if (e_x < 0 || e_x >= prm.mx) continue;
-            const float2 fe = X1[((e_y - b.EY0) * NEX + (e_x - b.EX0)) * NPE + (X - e_x * P) + (Y - e_y * P) * N1];
-            f[h][0] += fe.x; f[h][1] += fe.y;
-          }
-        }
-        for (int q = s0; q < s1; q++) {
-          const int sidx = prm.tile_src_idx[q], se = prm.src_elem[sidx], sx = se % prm.mx, sy = se / prm.mx;
-          const int a = X - sx * P, bb = Y - sy * P;
-          if (a >= 0 && a <= P && bb >= 0 && bb <= P) {
-            const float val = (float)prm.stf[sidx];
-            const float *sv = prm.src_vals + (size_t)sidx * 2 * NPE + 2 * (a + bb * N1);
-            f[h][0] = fmaf(val, sv[0], f[h][0]); f[h][1] = fmaf(val, sv[1], f[h][1]);
-          }
-        }
-      }
-      const float4 acc = make_float4(f[0][0] * minv_pre[k].x, f[0][1] * minv_pre[k].x,
-                                     f[1][0] * minv_pre[k].y, f[1][1] * minv_pre[k].y);
-      const int ri = (Y - b.RYa) * BXW + (XA - b.RXa);     // even: 16-byte aligned pairs
-      const int oi = oy * OBW + (XA - b.OXa);
-      float4 u = *reinterpret_cast<const float4 *>(rU + ri);
-      float4 w = *reinterpret_cast<const float4 *>(oW + oi);
-      float4 cu = KAHAN ? *reinterpret_cast<const float4 *>(rCU + ri) : make_float4(0.f, 0.f, 0.f, 0.f);
-      float4 cw = KAHAN ? *reinterpret_cast<const float4 *>(oCW + oi) : make_float4(0.f, 0.f, 0.f, 0.f);
-      if (r1 > r0) {
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-          if (!(h ? v1 : v0)) continue;
-          const int X = XA + h;
-          const float ux = h ? u.z : u.x, uy = h ? u.w : u.y, wx = h ? w.z : w.x, wy = h ? w.w : w.y;
-          const float ax = h ? acc.z : acc.x, ay = h ? acc.w : acc.y;
-          for (int q = r0; q < r1; q++) {
-            const int r = prm.tile_rec_idx[q], re = prm.rec_elem[r], rx = re % prm.mx, ry = re / prm.mx;
-            const int a = X - rx * P, bb = Y - ry * P;
-            if (a >= 0 && a <= P && bb >= 0 && bb <= P) {
-              float *rb = prm.rbuf_out + ((size_t)r * NPE + a + bb * N1) * 6;
-              rb[0] = ux; rb[1] = uy; rb[2] = fmaf(prm.half_dt, ax, wx); rb[3] = fmaf(prm.half_dt, ay, wy);
-              rb[4] = ax; rb[5] = ay;
-            }
-          }
-        }
-      }
-      if (KAHAN) {
-        kahan_add(w.x, cw.x, prm.dt * acc.x); kahan_add(w.y, cw.y, prm.dt * acc.y);
-        kahan_add(w.z, cw.z, prm.dt * acc.z); kahan_add(w.w, cw.w, prm.dt * acc.w);
-        kahan_add(u.x, cu.x, prm.dt * w.x); kahan_add(u.y, cu.y, prm.dt * w.y);
-        kahan_add(u.z, cu.z, prm.dt * w.z); kahan_add(u.w, cu.w, prm.dt * w.w);
-      } else {
-        w.x = fmaf(prm.dt, acc.x, w.x); w.y = fmaf(prm.dt, acc.y, w.y);
-        w.z = fmaf(prm.dt, acc.z, w.z); w.w = fmaf(prm.dt, acc.w, w.w);
-        u.x = fmaf(prm.dt, w.x, u.x); u.y = fmaf(prm.dt, w.y, u.y);
-        u.z = fmaf(prm.dt, w.z, u.z); u.w = fmaf(prm.dt, w.w, u.w);
-      }
-      const size_t n = (size_t)Y * prm.pitch + XA;
-      if (v0 && v1) {
-        *reinterpret_cast<float4 *>(prm.u_out + n) = u;
-        *reinterpret_cast<float4 *>(prm.w_out + n) = w;
-        if (KAHAN) { *reinterpret_cast<float4 *>(prm.cu_out + n) = cu; *reinterpret_cast<float4 *>(prm.cw_out + n) = cw; }
-        if (prm.a_out) *reinterpret_cast<float4 *>(prm.a_out + n) = acc;
-      } else {
-        const int h = v0 ? 0 : 1;
-        prm.u_out[n + h] = h ? make_float2(u.z, u.w) : make_float2(u.x, u.y);
-        prm.w_out[n + h] = h ? make_float2(w.z, w.w) : make_float2(w.x, w.y);
-        if (KAHAN) {
-          prm.cu_out[n + h] = h ? make_float2(cu.z, cu.w) : make_float2(cu.x, cu.y);
-          prm.cw_out[n + h] = h ? make_float2(cw.z, cw.w) : make_float2(cw.x, cw.y);
-        }
-        if (prm.a_out) prm.a_out[n + h] = h ? make_float2(acc.z, acc.w) : make_float2(acc.x, acc.y);
-      }
-    }
-    __syncthreads();   // stage s and the exchange buffers are free again
   }
+}
+
+// Many independent shots of one degree in one persistent launch.  The CTAs walk
+// a flattened (shot, tile) list.  Each shot's parameters come from a table in
+// global memory that depends only on which field buffer is the input; the
+// per-step pointers are derived from the step's index within its block (kblk):
+//   stf       = shot.stf + kblk * nsrc                     (block staging [shot][K][nsrc])
+//   rbuf out  = kblk even ? shot.rbuf_out : shot.rbuf_in  (receiver ping-pong)
+//   trace row = shot.trace_row + kblk * 7 * nrec           (block staging [shot][K][nrec][7])
+// so the launches of a block are the same on every repetition (graph replay).
+__device__ __forceinline__ const float *batch_rbuf(const Params &sh, int kblk)
+{
+  return (kblk & 1) ? sh.rbuf_in : sh.rbuf_out;
+}
+
+template <int P, int TE, int NT, bool KAHAN>
+__global__ void __launch_bounds__(NT, ((2 * (Layout<P, TE, KAHAN>::BATCH_TOTAL + 1024) <= 233472) ? 2 : 1))
+persist_batch(const BatchArgs ba)
+{
+  typedef Geo<P, TE> G;
+  typedef Layout<P, TE, KAHAN> L;
+  constexpr int N1 = G::N1, NEX = G::NEX;
+  static_assert(NT >= G::ITEMS, "one (element, line) item per thread");
+  static_assert(sizeof(Params) % 8 == 0, "Params copied in 8-byte words");
+  const float *D = c_D[P - 1];
+  const float *W = c_w[P - 1];
+  extern __shared__ __align__(128) unsigned char smem[];
+  unsigned char *stage0 = smem;
+  unsigned char *stage1 = smem + L::STAGE;
+  float2 *X1 = reinterpret_cast<float2 *>(smem + 2 * L::STAGE);
+  float2 *X2 = reinterpret_cast<float2 *>(smem + 2 * L::STAGE + L::XCH);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * L::STAGE + 2 * L::XCH);
+  const uint32_t bar0 = smem_u32(&bars[0]), bar1 = smem_u32(&bars[1]);
+  Params &sp = *reinterpret_cast<Params *>(smem + L::TOTAL);   // the current tile's shot, this step's pointers
+
+  if (threadIdx.x == 0) {
+    mbar_init(bar0, 1);
+    mbar_init(bar1, 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  // receivers of the previous step of this block, one CTA per shot
+  if (ba.kblk > 0)
+    for (int sh = blockIdx.x; sh < ba.nshots; sh += gridDim.x) {
+      const Params &q = ba.shots[sh];
+      if (q.nrec > 0) sample_rows<P>(q, batch_rbuf(q, ba.kblk - 1), q.trace_row + (size_t)(ba.kblk - 1) * 7 * q.nrec);
+    }
+
+  const int item = threadIdx.x;
+  const int el = item / N1, j = item - (item / N1) * N1;
+  const int ecy = el / NEX, ecx = el - (el / NEX) * NEX;
+  float Dcj[N1];
+#pragma unroll
+  for (int k = 0; k < N1; k++) Dcj[k] = (item < G::ITEMS) ? D[k * N1 + j] : 0.f;
+  const float wj = (item < G::ITEMS) ? W[j] : 0.f;
+
+  int w = blockIdx.x;
+  if (w < ba.nitems && threadIdx.x == 0) {
+    const int2 wt = ba.items[w];
+    const CUtensorMap *m = ba.maps + 4 * wt.x;
+    issue_tile<P, TE, KAHAN>(ba.shots[wt.x], wt.y, stage0, bar0, m, m + 1, m + 2, m + 3);
+  }
+  for (int it = 0; w < ba.nitems; it++, w += gridDim.x) {
+    const int s = it & 1;
+    const uint32_t bar = s ? bar1 : bar0;
+    const uint32_t parity = (it >> 1) & 1;
+    const int wn = w + gridDim.x;
+    const int2 wt = ba.items[w];
+    if (threadIdx.x < 32) {
+      // warp 0 copies the shot's parameters and patches this step's pointers
+      const uint64_t *src = reinterpret_cast<const uint64_t *>(&ba.shots[wt.x]);
+      uint64_t *dst = reinterpret_cast<uint64_t *>(&sp);
+      for (int i = threadIdx.x; i < (int)(sizeof(Params) / 8); i += 32) dst[i] = src[i];
+      __syncwarp();
+      if (threadIdx.x == 0) {
+        sp.stf = sp.stf + (size_t)ba.kblk * sp.nsrc;
+        sp.rbuf_out = const_cast<float *>(batch_rbuf(ba.shots[wt.x], ba.kblk));
+        if (!ba.write_a) sp.a_out = nullptr;
+        if (wn < ba.nitems) {
+          fence_proxy_async();
+          const int2 wnt = ba.items[wn];
+          const CUtensorMap *m = ba.maps + 4 * wnt.x;
+          issue_tile<P, TE, KAHAN>(ba.shots[wnt.x], wnt.y, s ? stage0 : stage1, s ? bar0 : bar1, m, m + 1, m + 2, m + 3);
+        }
+      }
+    }
+    __syncthreads();
+    if (!tile_body<P, TE, NT, KAHAN>(sp, wt.y, s ? stage1 : stage0, bar, parity, X1, X2, item, el, j, ecx, ecy, Dcj,
+                                     wj)) {
+      if (threadIdx.x == 0) {
+        atomicExch(ba.err, 1);
+        mbar_wait_bounded(bar, parity);
+        if (wn < ba.nitems) mbar_wait_bounded(s ? bar0 : bar1, ((it + 1) >> 1) & 1);
+      }
+      return;
+    }
+  }
+}
+
+// receivers of the last step (kblk) of a block of batched steps, one CTA per shot
+template <int P>
+__global__ void persist_record_batch(const Params *shots, int nshots, int kblk)
+{
+  if ((int)blockIdx.x >= nshots) return;
+  const Params &q = shots[blockIdx.x];
+  if (q.nrec > 0) sample_rows<P>(q, batch_rbuf(q, kblk), q.trace_row + (size_t)kblk * 7 * q.nrec);
 }
 
 // receiver rows of the last step of a block
 template <int P>
 __global__ void persist_record(const Params prm)
 {
-  sample_rows<P>(prm);
+  sample_rows<P>(prm, prm.rbuf_in, prm.trace_row);
 }
 
 }  // namespace se2p

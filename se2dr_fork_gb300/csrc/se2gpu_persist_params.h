@@ -1,5 +1,6 @@
 // se2gpu_persist_params.h -- launch parameters of the persistent FP32 step kernel.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace se2p {
@@ -32,6 +33,19 @@ struct Params {
   // per-tile lists (CSR over tiles) of the sources and receivers whose element
   // touches the tile's owned nodes, built on the host
   const int *tile_src_off, *tile_src_idx, *tile_rec_off, *tile_rec_idx;
+};
+
+// arguments of one batched step (many shots of one degree).  The shot table's
+// rbuf_out / rbuf_in are the shot's two receiver buffers (written at even / odd
+// steps of a block); stf and trace_row point at the shot's block staging.
+struct BatchArgs {
+  const Params *shots;         // per shot, for this step's input buffer
+  const CUtensorMap *maps;     // [shot][4]: region u, region cu, owned w, owned cw of the input buffers
+  const int2 *items;           // (shot, tile) work list
+  int nshots, nitems;
+  int kblk;                    // step index within the block
+  int write_a;                 // store a_k (last step of a block)
+  int *err;
 };
 
 }  // namespace se2p

@@ -24,7 +24,12 @@ PRECISIONS = {"fp64": FP64, "fp32_kahan": FP32_KAHAN, "fp32": FP32}
 EXPORTS = ["se2gpu_create", "se2gpu_destroy", "se2gpu_last_error", "se2gpu_create_error", "se2gpu_set_stream",
            "se2gpu_synchronize", "se2gpu_set_fields", "se2gpu_get_fields", "se2gpu_advance", "se2gpu_traces",
            "se2gpu_norms", "se2gpu_assemble_linear_form", "se2gpu_assemble_linear_form_device", "se2gpu_info",
-           "se2gpu_device_fields", "se2gpu_tile_configs", "se2gpu_set_tile_config"]
+           "se2gpu_device_fields", "se2gpu_tile_configs", "se2gpu_set_tile_config",
+           "se2gpu_ensemble_create", "se2gpu_ensemble_destroy", "se2gpu_ensemble_last_error",
+           "se2gpu_ensemble_set_stream", "se2gpu_ensemble_set_graphs", "se2gpu_ensemble_set_tile_config",
+           "se2gpu_ensemble_tile_config", "se2gpu_ensemble_advance", "se2gpu_ensemble_enqueue",
+           "se2gpu_ensemble_synchronize", "se2gpu_ensemble_get_fields", "se2gpu_ensemble_set_fields",
+           "se2gpu_ensemble_info"]
 
 
 class _CProblem(C.Structure):
@@ -68,6 +73,21 @@ def lib():
         L.se2gpu_device_fields.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]
         L.se2gpu_tile_configs.argtypes = [vp, _ip, _ip, C.c_int]
         L.se2gpu_set_tile_config.argtypes = [vp, C.c_int]
+        L.se2gpu_ensemble_create.argtypes = [C.POINTER(_CProblem), C.c_int, C.c_int, C.c_int, C.POINTER(vp)]
+        L.se2gpu_ensemble_destroy.argtypes = [vp]
+        L.se2gpu_ensemble_destroy.restype = None
+        L.se2gpu_ensemble_last_error.argtypes = [vp]
+        L.se2gpu_ensemble_last_error.restype = C.c_char_p
+        L.se2gpu_ensemble_set_stream.argtypes = [vp, vp]
+        L.se2gpu_ensemble_set_graphs.argtypes = [vp, C.c_int]
+        L.se2gpu_ensemble_set_tile_config.argtypes = [vp, C.c_int, C.c_int]
+        L.se2gpu_ensemble_tile_config.argtypes = [vp, C.c_int]
+        L.se2gpu_ensemble_advance.argtypes = [vp, C.c_int, _dp, _dp]
+        L.se2gpu_ensemble_enqueue.argtypes = [vp, C.c_int]
+        L.se2gpu_ensemble_synchronize.argtypes = [vp]
+        L.se2gpu_ensemble_get_fields.argtypes = [vp, C.c_int, _dp, _dp, _dp]
+        L.se2gpu_ensemble_set_fields.argtypes = [vp, C.c_int, _dp, _dp, _dp]
+        L.se2gpu_ensemble_info.argtypes = [vp, C.POINTER(C.c_long)]
         _lib = L
     return _lib
 
@@ -78,6 +98,19 @@ def _p(a: Optional[np.ndarray], t=_dp):
 
 class GpuError(RuntimeError):
     pass
+
+
+def _problem(s: Setup):
+    """se2gpu_problem of a host set-up, with the arrays it points into."""
+    keep = [np.ascontiguousarray(x) for x in (s.D.reshape(-1), s.wq, s.w1d, s.J00, s.J11, s.iJ00, s.iJ11,
+                                              s.lam, s.mu, s.mass, s.src_elem, s.src_vals.reshape(-1),
+                                              s.rec_node, s.rec_elem, s.rec_gll)]
+    (D, wq, w1d, J00, J11, iJ00, iJ11, lam, mu, mass, se, sv, rn, re, rg) = keep
+    pr = _CProblem(mx=s.mx, my=s.my, p=s.p, dt=s.dt, D=_p(D), wq=_p(wq), w1d=_p(w1d), J00=_p(J00), J11=_p(J11),
+                   iJ00=_p(iJ00), iJ11=_p(iJ11), lambda_=_p(lam), mu=_p(mu), mass=_p(mass),
+                   nsrc=s.nsrc, src_elem=_p(se, _ip), src_vals=_p(sv),
+                   nrec=s.nrec, rec_node=_p(rn, _ip), rec_elem=_p(re, _ip), rec_gll=_p(rg, _ip))
+    return pr, keep
 
 
 class Solver:
@@ -92,15 +125,8 @@ class Solver:
     def __init__(self, setup: Setup, precision="fp64", trace_capacity: Optional[int] = None):
         self.setup = setup
         self.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        pr, self._keep = _problem(setup)
         s = setup
-        self._keep = [np.ascontiguousarray(x) for x in (s.D.reshape(-1), s.wq, s.w1d, s.J00, s.J11, s.iJ00, s.iJ11,
-                                                       s.lam, s.mu, s.mass, s.src_elem, s.src_vals.reshape(-1),
-                                                       s.rec_node, s.rec_elem, s.rec_gll)]
-        (D, wq, w1d, J00, J11, iJ00, iJ11, lam, mu, mass, se, sv, rn, re, rg) = self._keep
-        pr = _CProblem(mx=s.mx, my=s.my, p=s.p, dt=s.dt, D=_p(D), wq=_p(wq), w1d=_p(w1d), J00=_p(J00), J11=_p(J11),
-                       iJ00=_p(iJ00), iJ11=_p(iJ11), lambda_=_p(lam), mu=_p(mu), mass=_p(mass),
-                       nsrc=s.nsrc, src_elem=_p(se, _ip), src_vals=_p(sv),
-                       nrec=s.nrec, rec_node=_p(rn, _ip), rec_elem=_p(re, _ip), rec_gll=_p(rg, _ip))
         if trace_capacity is None:
             trace_capacity = max(1, min(s.nsteps, 1 << 16)) if s.nrec else 0
         self.trace_capacity = int(trace_capacity)
@@ -221,3 +247,122 @@ class Solver:
     def set_tile_config(self, config: int):
         self._check(lib().se2gpu_set_tile_config(self._h, int(config)), "se2gpu_set_tile_config")
         self.tile_config = int(config)
+
+
+class Ensemble:
+    """Many independent shots advanced together by the batched persistent kernel
+    (se2gpu_ensemble_*): one launch per degree group per step, blocks of
+    `block` steps replayed as CUDA graphs.  FP32 precisions only; each shot
+    evolves bit-identically to a :class:`Solver` of the same set-up."""
+
+    def __init__(self, setups, precision="fp32_kahan", block: int = 100):
+        self.setups = list(setups)
+        self.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        n = len(self.setups)
+        arr = (_CProblem * n)()
+        self._keep = []
+        for i, su in enumerate(self.setups):
+            pr, keep = _problem(su)
+            arr[i] = pr
+            self._keep.append(keep)
+        h = C.c_void_p()
+        rc = lib().se2gpu_ensemble_create(arr, n, self.precision, int(block), C.byref(h))
+        self._keep = None   # the library copied everything it needs
+        if rc != 0:
+            raise GpuError(f"se2gpu_ensemble_create failed ({rc}): {lib().se2gpu_ensemble_last_error(None).decode()}")
+        self._h = h
+        self.block = int(block)
+        self.nsrc = np.array([su.nsrc for su in self.setups])
+        self.nrec = np.array([su.nrec for su in self.setups])
+        self.time = np.zeros(n)
+        self.step = 0
+
+    def _check(self, rc: int, what: str) -> int:
+        if rc < 0:
+            raise GpuError(f"{what} failed ({rc}): {lib().se2gpu_ensemble_last_error(self._h).decode()}")
+        return rc
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().se2gpu_ensemble_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __len__(self):
+        return len(self.setups)
+
+    def stf(self, nsteps: int):
+        """Host STF values of the next nsteps steps, shot-major, and each shot's times."""
+        vals, times, ends = [], [], []
+        for i, su in enumerate(self.setups):
+            t, v, t_end = su.stf_block(self.time[i], nsteps)
+            vals.append(v.reshape(-1))
+            times.append(t)
+            ends.append(t_end)
+        return np.ascontiguousarray(np.concatenate(vals) if vals else np.zeros(0)), times, np.array(ends)
+
+    def advance(self, nsteps: int, stf: Optional[np.ndarray] = None, traces: bool = True):
+        """Advance every shot; returns per shot the receiver rows [time, 7 per receiver] (or None)."""
+        if nsteps <= 0:
+            return [np.zeros((0, 1 + 7 * r)) for r in self.nrec] if traces else None
+        auto, times, ends = self.stf(nsteps)
+        stf = auto if stf is None else np.ascontiguousarray(stf, dtype=np.float64).reshape(-1)
+        out = np.zeros(max(1, nsteps * 7 * int(self.nrec.sum()))) if traces else None
+        self._check(lib().se2gpu_ensemble_advance(self._h, int(nsteps), _p(stf) if stf.size else None, _p(out)),
+                    "se2gpu_ensemble_advance")
+        self.time = ends
+        self.step += nsteps
+        if not traces:
+            return None
+        res, off = [], 0
+        for i, r in enumerate(self.nrec):
+            blk = out[off: off + nsteps * 7 * r].reshape(nsteps, 7 * r)
+            res.append(np.concatenate([times[i].reshape(-1, 1), blk], axis=1))
+            off += nsteps * 7 * r
+        return res
+
+    def enqueue(self, nsteps: int):
+        self._check(lib().se2gpu_ensemble_enqueue(self._h, int(nsteps)), "se2gpu_ensemble_enqueue")
+        self.step += nsteps
+
+    def synchronize(self):
+        self._check(lib().se2gpu_ensemble_synchronize(self._h), "se2gpu_ensemble_synchronize")
+
+    def set_stream(self, stream_ptr: int):
+        self._check(lib().se2gpu_ensemble_set_stream(self._h, C.c_void_p(stream_ptr)), "se2gpu_ensemble_set_stream")
+
+    def set_graphs(self, enable: bool):
+        self._check(lib().se2gpu_ensemble_set_graphs(self._h, int(bool(enable))), "se2gpu_ensemble_set_graphs")
+
+    def set_tile_config(self, p: int, config: int):
+        self._check(lib().se2gpu_ensemble_set_tile_config(self._h, int(p), int(config)),
+                    "se2gpu_ensemble_set_tile_config")
+
+    def tile_config(self, p: int) -> int:
+        return self._check(lib().se2gpu_ensemble_tile_config(self._h, int(p)), "se2gpu_ensemble_tile_config")
+
+    def degrees(self):
+        return sorted({su.p for su in self.setups})
+
+    def fields(self, shot: int):
+        if not 0 <= shot < len(self.setups):   # let the library report the bad index
+            self._check(lib().se2gpu_ensemble_get_fields(self._h, int(shot), None, None, None),
+                        "se2gpu_ensemble_get_fields")
+        n = self.setups[shot].ndof
+        u, v, a = np.zeros(n), np.zeros(n), np.zeros(n)
+        self._check(lib().se2gpu_ensemble_get_fields(self._h, int(shot), _p(u), _p(v), _p(a)),
+                    "se2gpu_ensemble_get_fields")
+        return u, v, a
+
+    def set_fields(self, shot: int, u=None, v=None, a=None):
+        arrs = [None if x is None else np.ascontiguousarray(x, dtype=np.float64) for x in (u, v, a)]
+        self._check(lib().se2gpu_ensemble_set_fields(self._h, int(shot), *[_p(x) for x in arrs]),
+                    "se2gpu_ensemble_set_fields")
+
+    def info(self) -> dict:
+        a = (C.c_long * 9)()
+        self._check(lib().se2gpu_ensemble_info(self._h, a), "se2gpu_ensemble_info")
+        keys = ["shots", "groups", "block", "launches", "replays", "nodes", "sources", "receivers", "items"]
+        return dict(zip(keys, list(a)))

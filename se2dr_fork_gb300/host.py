@@ -42,6 +42,14 @@ class _CSetup(C.Structure):
                 ("nrec", C.c_int), ("rec_xy", _dp), ("rec_node", _ip), ("rec_elem", _ip), ("rec_gll", _ip)]
 
 
+class CShotDraw(C.Structure):
+    _fields_ = [("mx", C.c_int), ("my", C.c_int), ("p", C.c_int), ("nrec", C.c_int), ("nsteps", C.c_long),
+                ("h", C.c_double), ("Lx", C.c_double), ("Ly", C.c_double), ("interface_y", C.c_double),
+                ("lower", C.c_double * 3), ("upper", C.c_double * 3), ("ninc", C.c_int),
+                ("inc", (C.c_double * 8) * 2), ("src_xy", C.c_double * 2), ("moment", C.c_double * 4),
+                ("f0", C.c_double), ("t0", C.c_double)]
+
+
 _lib = None
 
 
@@ -61,6 +69,8 @@ def lib():
         L.se2_stf_eval.argtypes = [C.c_int, _dp, C.c_double, _dp]
         L.se2_gaussian_random_field.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                                 C.c_ulonglong, _dp]
+        L.se2_shot_draw_params.argtypes = [C.c_ulonglong, C.c_long, C.c_int, C.POINTER(CShotDraw)]
+        L.se2_shot_materials.argtypes = [C.POINTER(CShotDraw), _dp, _dp, _dp]
         _lib = L
     return _lib
 
@@ -200,3 +210,23 @@ def gaussian_random_field(mx: int, my: int, mean: float = 5000.0, rel_std: float
     if lib().se2_gaussian_random_field(mx, my, mean, rel_std, corr_cells, seed, _p(out)) != 0:
         raise ValueError(_err())
     return out
+
+
+SHOT_ENSEMBLE, SHOT_TRAINING, SHOT_OOD = 0, 1, 2
+
+
+def shot_draw(seed: int, index: int, kind: int = SHOT_ENSEMBLE) -> CShotDraw:
+    """Seeded draw of one shot's mesh, materials, source and wavelet (se2_shot_draw_params)."""
+    d = CShotDraw()
+    if lib().se2_shot_draw_params(seed, index, kind, C.byref(d)) != 0:
+        raise ValueError(_err())
+    return d
+
+
+def shot_materials(d: CShotDraw) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """Per-cell (vp, vs, rho) of a drawn shot (2 layers + elliptical inclusions)."""
+    n = d.mx * d.my
+    vp, vs, rho = np.zeros(n), np.zeros(n), np.zeros(n)
+    if lib().se2_shot_materials(C.byref(d), _p(vp), _p(vs), _p(rho)) != 0:
+        raise ValueError(_err())
+    return vp, vs, rho

@@ -16,6 +16,10 @@ Named workloads:
   seeded Gaussian random field (mean 5000 m/s, 10 % std, correlation length 8
   cells), Vp/Vs = 1.73, rho = 2700, same explosive source with Ricker f0 = 8 Hz,
   t0 = 0.15 s, 64 receivers on a horizontal line, 20000 steps at 0.2 CFL.
+* :func:`shot` -- one seeded draw of the ensemble / surrogate distributions:
+  2-layer + elliptical-inclusion materials, random source position, symmetric
+  moment tensor with N(0, 1e15) entries, Ricker f0 ~ U[5, 20] Hz; receivers on
+  the top surface.  :func:`ensemble` is a list of such draws.
 """
 from __future__ import annotations
 
@@ -146,3 +150,37 @@ def grf2048(mx: int = 2048, my: Optional[int] = None, p: int = 4, nt: int = 2000
                 cfl=0.2, tmax=1.0e30, nt=nt, name="grf2048",
                 sources=[Source(0.0, 0.0, (1e15, 0.0, 0.0, 1e15), STF_RICKER, (0.15, 8.0, 1.0))],
                 receivers=rec)
+
+
+def shot(seed: int, index: int, kind: int = 0, nt: Optional[int] = None, p: Optional[int] = None,
+         size: Optional[Tuple[int, int]] = None) -> Spec:
+    """Shot `index` of the seeded distribution `kind` (0 ensemble, 1 training, 2 out-of-distribution),
+    drawn by the host library's C generator.  Domain [0, Lx] x [0, Ly], 31.25 m elements, dt = 0.2 CFL.
+    `size` = (mx, my) replaces the drawn mesh, with the geometry scaled along (small test cases)."""
+    from . import host
+    d = host.shot_draw(seed, index, kind)
+    if size is not None:
+        fx, fy = size[0] / d.mx, size[1] / d.my
+        d.mx, d.my = int(size[0]), int(size[1])
+        d.Lx, d.Ly = d.mx * d.h, d.my * d.h
+        d.interface_y *= fy
+        for i in range(d.ninc):
+            d.inc[i][0] *= fx; d.inc[i][1] *= fy; d.inc[i][2] *= fx; d.inc[i][3] *= fy
+        d.src_xy[0] *= fx
+        d.src_xy[1] *= fy
+    vp, vs, rho = host.shot_materials(d)
+    Lx, Ly = d.Lx, d.Ly
+    yr = Ly - 1.0e-3        # 1 mm below the top surface: the receivers snap to the surface nodes
+    rec = [(float(x), float(yr)) for x in np.linspace(0.05 * Lx, 0.95 * Lx, d.nrec)]
+    src = Source(float(d.src_xy[0]), float(d.src_xy[1]), tuple(float(m) for m in d.moment), STF_RICKER,
+                 (float(d.t0), float(d.f0), 1.0))
+    return Spec(mx=d.mx, my=d.my, p=d.p if p is None else p, scale=(Lx, Ly), shift=(0.0, 0.0),
+                vp=float(vp.mean()), vs=float(vs.mean()), rho=float(rho.mean()),
+                cell_vp=vp, cell_vs=vs, cell_rho=rho, cfl=0.2, tmax=1.0e30,
+                nt=int(d.nsteps if nt is None else nt), name=f"shot{kind}_{seed}_{index}",
+                sources=[src], receivers=rec)
+
+
+def ensemble(nshots: int = 256, seed: int = 3, kind: int = 0, nt: Optional[int] = None) -> List[Spec]:
+    """The batched-ensemble workload: `nshots` seeded draws (256 shots, 5000 steps by default)."""
+    return [shot(seed, i, kind, nt) for i in range(nshots)]

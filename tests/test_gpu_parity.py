@@ -8,7 +8,7 @@ receiver traces (the tolerance the target states for FP32).
 import numpy as np
 import pytest
 
-from golden_util import load, spec_of
+from golden_util import FP32_COMPONENT_TOL, K_SHEAR, fp32_errors, fp32_errors_ok, load, rel_l2, spec_of
 from oracle import oracle as O
 from se2dr_fork_gb300 import gpu as G
 from se2dr_fork_gb300 import host as H
@@ -17,34 +17,6 @@ from se2dr_fork_gb300 import spec as S
 pytestmark = pytest.mark.gpu
 
 FP32_TOL = 1e-5
-# FP32 error bars per trace component (ux uy vx vy ax ay curl): the 1e-5 target
-# holds for displacement; acceleration and curl(v) are second and first spatial
-# derivatives of an FP32-rounded field, which the stiffness operator amplifies
-# by ~(p^2 lambda / 2 pi h)^2 and ~(p^2 lambda / 2 pi h).
-FP32_COMPONENT_TOL = (1e-5, 1e-5, 1e-4, 1e-4, 5e-3, 5e-3, 5e-3)
-# curl(v) is compared on the scale of the velocity gradient, k |v| with the shear
-# wavenumber of the source's peak frequency: an explosive source radiates P waves,
-# whose curl is pure discretisation noise (1e-11 k|v| in FP64), so a relative
-# error of the curl itself would not measure anything.
-K_SHEAR = 2.0 * np.pi * 10.0 / 3464.0
-
-
-def fp32_errors(tr32, tr64, k=K_SHEAR):
-    errs = [rel_l2(tr32[:, 1 + c::7], tr64[:, 1 + c::7]) for c in range(6)]
-    v = tr64[:, 3::7], tr64[:, 4::7]
-    scale = max(np.linalg.norm(tr64[:, 7::7]), k * np.sqrt(np.linalg.norm(v[0]) ** 2 + np.linalg.norm(v[1]) ** 2))
-    errs.append(np.linalg.norm(tr32[:, 7::7] - tr64[:, 7::7]) / scale)
-    return errs
-
-
-def fp32_errors_ok(tr32, tr64, k=K_SHEAR):
-    errs = fp32_errors(tr32, tr64, k)
-    return all(e <= t for e, t in zip(errs, FP32_COMPONENT_TOL)), errs
-
-
-def rel_l2(x, ref):
-    den = np.linalg.norm(ref)
-    return np.linalg.norm(x - ref) / (den if den > 0 else 1.0)
 
 
 @pytest.fixture(scope="module", autouse=True)
