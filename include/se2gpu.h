@@ -161,6 +161,22 @@ int se2gpu_ensemble_set_fields(se2gpu_ensemble *e, int shot, const double *u, co
    replays, total nodes, total sources, total receivers, (shot, tile) items. */
 int se2gpu_ensemble_info(const se2gpu_ensemble *e, long *ints);
 
+/* ---- Norms without device allocation.  No counterpart in the reference (its
+   VecMax/VecMin/VecNorm log lines come from PETSc on host vectors).
+   out[6] = max, min, l2 of u then of v (as se2gpu_norms) for n FP64 values of
+   caller-owned device vectors u_dev, v_dev, computed on `stream` (a
+   cudaStream_t; NULL = the legacy default stream); returns after the result is
+   in `out`.  Allocates nothing: the per-block partials use a fixed static device
+   array of SE2GPU_NOALLOC_MAX_BLOCKS x 6 doubles (192 KiB), so n may not exceed
+   SE2GPU_NOALLOC_MAX_VALUES (larger n is rejected with SE2GPU_ERR_ARG).  The
+   first call on each device looks up that array's address and should come
+   before any stream capture.  Calls that overlap in time share the array and
+   race.  On failure se2gpu_last_error(NULL) gives the message. */
+#define SE2GPU_NOALLOC_CHUNK 65536L
+#define SE2GPU_NOALLOC_MAX_BLOCKS 4096
+#define SE2GPU_NOALLOC_MAX_VALUES (SE2GPU_NOALLOC_CHUNK * SE2GPU_NOALLOC_MAX_BLOCKS)
+int se2gpu_norms_device_noalloc(const double *u_dev, const double *v_dev, long n, void *stream, double out[6]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -28,6 +28,7 @@
 static thread_local char g_create_err[512];
 
 extern "C" const char *se2gpu_create_error(void) { return g_create_err; }
+void se2gpu_internal_set_error(const char *msg) { snprintf(g_create_err, sizeof(g_create_err), "%s", msg); }
 extern "C" const char *se2gpu_last_error(const se2gpu_solver *h) { return h ? h->err : g_create_err; }
 
 static int fail(se2gpu_solver *h, int code, const char *fmt, ...)

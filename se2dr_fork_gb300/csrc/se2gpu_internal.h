@@ -45,3 +45,5 @@ struct se2gpu_solver {
 
 // FP32 persistent-kernel parameters of a handle (no per-step pointers set)
 se2p::Params se2gpu_internal_f32_params(se2gpu_solver *h);
+// set the thread's message returned by se2gpu_last_error(NULL)
+void se2gpu_internal_set_error(const char *msg);

@@ -29,7 +29,7 @@ EXPORTS = ["se2gpu_create", "se2gpu_destroy", "se2gpu_last_error", "se2gpu_creat
            "se2gpu_ensemble_set_stream", "se2gpu_ensemble_set_graphs", "se2gpu_ensemble_set_tile_config",
            "se2gpu_ensemble_tile_config", "se2gpu_ensemble_advance", "se2gpu_ensemble_enqueue",
            "se2gpu_ensemble_synchronize", "se2gpu_ensemble_get_fields", "se2gpu_ensemble_set_fields",
-           "se2gpu_ensemble_info"]
+           "se2gpu_ensemble_info", "se2gpu_norms_device_noalloc"]
 
 
 class _CProblem(C.Structure):
@@ -88,6 +88,7 @@ def lib():
         L.se2gpu_ensemble_get_fields.argtypes = [vp, C.c_int, _dp, _dp, _dp]
         L.se2gpu_ensemble_set_fields.argtypes = [vp, C.c_int, _dp, _dp, _dp]
         L.se2gpu_ensemble_info.argtypes = [vp, C.POINTER(C.c_long)]
+        L.se2gpu_norms_device_noalloc.argtypes = [vp, vp, C.c_long, vp, _dp]
         _lib = L
     return _lib
 
