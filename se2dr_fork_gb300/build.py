@@ -2,6 +2,7 @@
 
 * ``lib/libse2host.so``  -- FP64 host set-up (C, gcc), include/se2host.h
 * ``lib/libse2gpu.so``   -- sm_103a kernels + C-ABI (nvcc), include/se2gpu.h
+* ``lib/libse2nn.so``    -- the surrogate network runtime (nvcc), include/se2nn.h
 * ``bin/se2wave_gpu``    -- the C host application (se2wave's command line)
 
 Each translation unit is compiled in parallel and only when its sources are
@@ -57,14 +58,25 @@ def build_host(force: bool = False) -> str:
     return out
 
 
+NN_UNITS = ["se2nn"]
+NN_DEPS = ["se2nn_gemm.cuh"]
+
+
 def build_gpu(force: bool = False) -> str:
+    return _build_cuda_lib("libse2gpu.so", CU_UNITS, [os.path.join(CSRC, d) for d in CU_DEPS] + [os.path.join(INC, "se2gpu.h")], force)
+
+
+def build_nn(force: bool = False) -> str:
+    return _build_cuda_lib("libse2nn.so", NN_UNITS, [os.path.join(CSRC, d) for d in NN_DEPS] + [os.path.join(INC, "se2nn.h")], force)
+
+
+def _build_cuda_lib(name: str, units, deps, force: bool) -> str:
     os.makedirs(LIB, exist_ok=True)
     os.makedirs(OBJ, exist_ok=True)
-    out = os.path.join(LIB, "libse2gpu.so")
-    deps = [os.path.join(CSRC, d) for d in CU_DEPS] + [os.path.join(INC, "se2gpu.h")]
+    out = os.path.join(LIB, name)
     jobs = []
     objs = []
-    for u in CU_UNITS:
+    for u in units:
         src = os.path.join(CSRC, u + ".cu")
         obj = os.path.join(OBJ, u + ".o")
         objs.append(obj)
@@ -92,12 +104,13 @@ def build_app(force: bool = False) -> str:
 
 
 def build_all(force: bool = False) -> dict:
-    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+    with cf.ThreadPoolExecutor(max_workers=3) as ex:
         fh = ex.submit(build_host, force)
         fg = ex.submit(build_gpu, force)
-        host, gpu = fh.result(), fg.result()
+        fn = ex.submit(build_nn, force)
+        host, gpu, nn = fh.result(), fg.result(), fn.result()
     app = build_app(force)
-    return {"host": host, "gpu": gpu, "app": app}
+    return {"host": host, "gpu": gpu, "nn": nn, "app": app}
 
 
 if __name__ == "__main__":

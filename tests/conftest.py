@@ -28,3 +28,11 @@ def gpu_lib():
     B.build_gpu()
     from se2dr_fork_gb300 import gpu
     return gpu.lib()
+
+
+@pytest.fixture(scope="session")
+def nn_lib():
+    from se2dr_fork_gb300 import build as B
+    B.build_nn()
+    from se2dr_fork_gb300 import nn
+    return nn.lib()

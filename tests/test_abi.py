@@ -25,6 +25,15 @@ def test_gpu_library_exports(gpu_lib):
     assert sorted(gpu.EXPORTS) == names
 
 
+def test_nn_library_exports(nn_lib):
+    from se2dr_fork_gb300 import nn
+    names = declared("se2nn.h")
+    assert sorted(nn.EXPORTS) == names
+    lib = nn_lib
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
 def test_host_library_exports():
     from se2dr_fork_gb300 import host
     names = declared("se2host.h")
