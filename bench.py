@@ -418,6 +418,75 @@ def run_ensemble(args):
     print(json.dumps(line), flush=True)
 
 
+def run_surrogate(args):
+    """Surrogate workload: training data from the batched FP32 solver, an ensemble of networks trained
+    with the project's BF16 kernels, held-out misfit, and serving with the disagreement gate + solver
+    fallback against the plain batched solver on the same draws.  Prints one JSON line."""
+    import torch
+    from se2dr_fork_gb300 import host as H
+    from se2dr_fork_gb300 import surrogate as SU
+    torch.cuda.set_device(0)
+    log = (lambda m: print(m, file=sys.stderr, flush=True))
+    t0 = time.perf_counter()
+    tr = SU.generate(4, args.train, H.SHOT_TRAINING)
+    log(f"training data: {args.train} draws in {tr.wall_seconds:.1f} s (solver {tr.seconds:.1f} s)")
+    nood = max(1, int(round(0.1 * args.test)))
+    te_in = SU.generate(5, args.test, H.SHOT_TRAINING)
+    te_ood = SU.generate(6, nood, H.SHOT_OOD)
+    test = SU.concat(te_in, te_ood)
+    t_data = time.perf_counter() - t0
+    dtrain = SU.DeviceData(tr, augment=True)
+    dtest = SU.DeviceData(test, scale=dtrain.scale)
+    rec_x = SU.receiver_cells(tr.specs[0])
+    nets, stats = [], []
+    for k in range(args.members):
+        net, st = SU.train(dtrain, np.arange(dtrain.n), rec_x, seed=k, epochs=args.epochs, batch=32, lr=args.lr,
+                           log=log)
+        nets.append(net)
+        stats.append(st)
+    fwd = SU.forward_flops(SU.net_config())
+    # inference throughput of one member (device-timed)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    tq = time.perf_counter()
+    preds = SU.predict(nets, dtest, np.arange(dtest.n))
+    t_pred = time.perf_counter() - tq
+    mean, dis = preds.mean(axis=0), SU.disagreement(preds)
+    mis = SU.rel_l2(mean, test.traces)
+    is_ood = test.kind == H.SHOT_OOD
+    what_if = []
+    for th in (0.01, 0.02, 0.05, 0.1, 0.2, 0.5):
+        acc = dis <= th
+        what_if.append({"threshold": th, "fallback_rate": float(1 - acc.mean()),
+                        "accepted_misfit_max": float(mis[acc].max()) if acc.any() else None,
+                        "accepted_misfit_mean": float(mis[acc].mean()) if acc.any() else None})
+    served = SU.serve(nets, dtest, test.specs, threshold=args.threshold, audit=0.05)
+    solver_sps = dtest.n / test.wall_seconds
+    line = {"metric": "seismograms/s surrogate vs solver @1% L2", "value": served["seismograms_per_s"],
+            "unit": "seismograms/s", "n_gpus": 1, "higher_is_better": True, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": f"{args.train} training draws, {args.test} held-out + {nood} out-of-distribution "
+                                   "requests; 128x128 elements, degree 4, 4096 steps, 16 receivers x 2 x 1024",
+                       "network": "4 Fourier layers, width 64, 16 modes; column decoder 64-128-16 (GELU)",
+                       "augmentation": "mirror in x (exact)", "members": args.members,
+                       "epochs": args.epochs, "batch": 32},
+            "solver_seismograms_per_s": solver_sps,
+            "speedup_vs_solver": served["seismograms_per_s"] / solver_sps,
+            "serving": served,
+            "held_out": {"misfit_mean": float(mis[~is_ood].mean()), "misfit_median": float(np.median(mis[~is_ood])),
+                         "misfit_p90": float(np.percentile(mis[~is_ood], 90)),
+                         "ood_misfit_mean": float(mis[is_ood].mean()),
+                         "disagreement_mean": float(dis[~is_ood].mean()), "ood_disagreement_mean": float(dis[is_ood].mean()),
+                         "corr_disagreement_misfit": float(np.corrcoef(dis, mis)[0, 1])},
+            "what_if": what_if,
+            "training": {"samples_per_s": [st["samples_per_s"] for st in stats],
+                         "tflops": [3 * fwd * st["samples_per_s"] / 1e12 for st in stats],
+                         "final_loss": [st["loss"][-1] for st in stats], "loss_curve_member0": stats[0]["loss"]},
+            "inference": {"samples_per_s": dtest.n * args.members / t_pred,
+                          "tflops": fwd * dtest.n * args.members / t_pred / 1e12},
+            "data_seconds": t_data, "train_data_solver_seconds": tr.seconds}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -436,6 +505,13 @@ def main():
     ap.add_argument("--ensemble", action="store_true", help="batched ensemble of --shots shots instead of the headline run")
     ap.add_argument("--shots", type=int, default=256)
     ap.add_argument("--block", type=int, default=100, help="ensemble steps per CUDA graph")
+    ap.add_argument("--surrogate", action="store_true", help="surrogate training + serving instead of the headline run")
+    ap.add_argument("--train", type=int, default=4000, help="surrogate training draws")
+    ap.add_argument("--test", type=int, default=500, help="surrogate held-out requests (+10%% out of distribution)")
+    ap.add_argument("--members", type=int, default=4)
+    ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--threshold", type=float, default=0.01)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -445,6 +521,8 @@ def main():
         run_sweep(args)
     elif args.ensemble and args.impl == "ours":
         run_ensemble(args)
+    elif args.surrogate and args.impl == "ours":
+        run_surrogate(args)
     elif args.impl == "reference":
         run_reference(args, rank, world)
     else:

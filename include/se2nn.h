@@ -4,7 +4,8 @@
 
    No counterpart in the reference (se2wave.c has no learned component).  The
    network maps the cell-wise material field plus a source channel to receiver
-   traces:
+   traces.  Grid rows count down from the top surface (row 0), so the time axis
+   of a receiver's trace lies along its column:
 
      input   x[b][y][x][cin]            BF16, channels last (cin a multiple of 16;
                                         the caller fills the used channels, the rest 0)
@@ -13,14 +14,13 @@
              S_l = spectral convolution: truncated real 2-D DFT keeping kx in
              [0, modes) and ky in [-modes, modes), per-mode complex width x width
              mixing, inverse DFT (1 / (nx ny) normalisation, Hermitian weights)
-     decoder per receiver r at top-row cell rec_x[r]:
-             d = [h[b][ny-1][rec_x[r]][:], mean over cells of h[b]]   (2 width)
-             out[b][r][:] = GELU(d W1 + c1) W2 + c2                    (nout values)
+     decoder for receiver r (column rec_x[r]) and every row y, nsub = nout / ny:
+             out[b][r][y][0:nsub] = GELU(h[b][y][rec_x[r]] W1 + c1) W2 + c2
 
    Parameters, as one FP32 vector in this order:
      W0 [cin][width], b0 [width];
      per layer: Wre [2 modes][modes][width][width], Wim (same), W [width][width], b [width];
-     W1 [2 width][hidden], c1 [hidden], W2 [hidden][nout], c2 [nout].
+     W1 [width][hidden], c1 [hidden], W2 [hidden][nsub], c2 [nsub].
    Mode (j, kx): ky = j for j < modes, ky = j - 2 modes (negative) otherwise.
 
    All pointers named *_dev are device memory; the others are host memory.
@@ -38,8 +38,8 @@ typedef struct se2nn_config {
   int modes;         /* retained modes per axis (16); 2 modes <= ny, modes <= nx / 2 */
   int layers;        /* Fourier layers (4) */
   int nrec;          /* receivers (16) */
-  int nout;          /* outputs per receiver (2 components x 1024 samples) */
-  int hidden;        /* decoder hidden width (256) */
+  int nout;          /* outputs per receiver, a multiple of ny (2 components x 1024 samples) */
+  int hidden;        /* decoder hidden width (128) */
   int max_batch;     /* largest batch of one call */
 } se2nn_config;
 
@@ -59,7 +59,7 @@ int se2nn_get_grads(se2nn *h, float *grads);
 /* top-row cell index of each receiver (nrec ints in [0, nx)) */
 int se2nn_set_receivers(se2nn *h, const int *rec_x);
 
-/* out_dev[b][r][nout] (FP32) = network(x_dev[b]) for b < batch */
+/* out_dev[b][r][ny][nout / ny] (FP32) = network(x_dev[b]) for b < batch */
 int se2nn_forward(se2nn *h, const void *x_dev, int batch, float *out_dev);
 
 /* Forward and backward of the mean-squared error against target_dev[b][r][nout]
@@ -73,11 +73,13 @@ int se2nn_loss_grad(se2nn *h, const void *x_dev, int batch, const float *target_
 int se2nn_adam_step(se2nn *h, float lr, float beta1, float beta2, float eps, float weight_decay);
 
 /* Input assembly from a resident data set: for b < batch, sample s = idx_dev[b]:
-   channels 0..2 = normalised (vp, vs, rho) of materials_dev[s][y][x][3] (FP32 m/s, m/s,
-   kg/m^3; (vp - 5000) / 1500, (vs - 2800) / 800, (rho - 2500) / 500),
-   channel 3 = exp(-|cell - src_dev[s]|^2 / (2 sigma^2)) with the source position
-   in cells (src_dev[s][2], x then y), channels 4, 5 = cell-centre coordinates in
-   [-1, 1], the rest 0.  x_dev[b][y][x][cin] (BF16). */
+   materials_dev[s][y][x][3] holds (vp, vs, rho) per cell (FP32 m/s, m/s, kg/m^3)
+   with row y counted up from the bottom, src_dev[s] the source position in cells
+   (x, y up from the bottom).  Network row yn is material row ny - 1 - yn:
+   channels 0..2 = (vp - 5000) / 1500, (vs - 2800) / 800, (rho - 2500) / 500,
+   channel 3 = exp(-|cell centre - source|^2 / (2 sigma^2)) (source at row
+   coordinate ny - y), channels 4, 5 = cell-centre coordinates in [-1, 1] (x, yn),
+   the rest 0.  x_dev[b][yn][x][cin] (BF16). */
 int se2nn_build_inputs(se2nn *h, const void *materials_dev, const float *src_dev, const int *idx_dev, int batch,
                        float sigma_cells, void *x_dev);
 

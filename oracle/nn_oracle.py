@@ -27,7 +27,7 @@ class Config:
     layers: int = 4
     nrec: int = 16
     nout: int = 2048
-    hidden: int = 256
+    hidden: int = 128
     max_batch: int = 32
 
 
@@ -37,7 +37,8 @@ def layout(c: Config):
     items = [("Wlift", (c.cin, w)), ("blift", (w,))]
     for l in range(c.layers):
         items += [(f"Wre{l}", (2 * m, m, w, w)), (f"Wim{l}", (2 * m, m, w, w)), (f"W{l}", (w, w)), (f"b{l}", (w,))]
-    items += [("Wdec1", (2 * w, c.hidden)), ("cdec1", (c.hidden,)), ("Wdec2", (c.hidden, c.nout)), ("cdec2", (c.nout,))]
+    ns = c.nout // c.ny
+    items += [("Wdec1", (w, c.hidden)), ("cdec1", (c.hidden,)), ("Wdec2", (c.hidden, ns)), ("cdec2", (ns,))]
     out, o = {}, 0
     for name, shape in items:
         n = int(np.prod(shape))
@@ -114,12 +115,10 @@ def forward(p: np.ndarray, x: np.ndarray, c: Config, rec_x, keep: bool = False):
         As.append(a)
         Zs.append(Z)
         Hs.append(h)
-    G = h.mean(axis=(1, 2))                                    # [B, w]
-    R = h[:, c.ny - 1, rec_x, :]                                # [B, nrec, w]
-    D0 = np.concatenate([R, np.broadcast_to(G[:, None, :], R.shape)], axis=2)
+    D0 = h[:, :, rec_x, :].transpose(0, 2, 1, 3)             # [B, nrec, ny, w]: each receiver's column
     D1pre = D0 @ P["Wdec1"] + P["cdec1"]
     D1 = gelu(D1pre)
-    out = D1 @ P["Wdec2"] + P["cdec2"]
+    out = (D1 @ P["Wdec2"] + P["cdec2"]).reshape(x.shape[0], len(rec_x), -1)   # [B, nrec, ny * nsub]
     if keep:
         return out, dict(P=P, mats=mats, x=x, Hs=Hs, As=As, Zs=Zs, D0=D0, D1pre=D1pre, D1=D1, rec_x=rec_x)
     return out
@@ -132,19 +131,17 @@ def loss_grad(p: np.ndarray, x: np.ndarray, target: np.ndarray, c: Config, rec_x
     diff = out - target
     loss = float(np.mean(diff * diff))
     g = {}
-    dout = 2.0 * diff / diff.size
-    g["Wdec2"] = np.einsum("bri,bro->io", k["D1"], dout)
-    g["cdec2"] = dout.sum(axis=(0, 1))
+    dout = (2.0 * diff / diff.size).reshape(k["D1"].shape[:3] + (-1,))
+    g["Wdec2"] = np.einsum("bryi,bryo->io", k["D1"], dout)
+    g["cdec2"] = dout.sum(axis=(0, 1, 2))
     dD1pre = (dout @ P["Wdec2"].T) * gelu_grad(k["D1pre"])
-    g["Wdec1"] = np.einsum("bri,bro->io", k["D0"], dD1pre)
-    g["cdec1"] = dD1pre.sum(axis=(0, 1))
-    dD0 = dD1pre @ P["Wdec1"].T
-    w = c.width
+    g["Wdec1"] = np.einsum("bryi,bryo->io", k["D0"], dD1pre)
+    g["cdec1"] = dD1pre.sum(axis=(0, 1, 2))
+    dD0 = dD1pre @ P["Wdec1"].T                                # [B, nrec, ny, w]
     B = x.shape[0]
     dh = np.zeros_like(k["Hs"][-1])
-    dh += dD0[:, :, w:].sum(axis=1)[:, None, None, :] / (c.ny * c.nx)
     for r, rx in enumerate(k["rec_x"]):
-        dh[:, c.ny - 1, rx, :] += dD0[:, r, :w]
+        dh[:, :, rx, :] += dD0[:, r]
     for l in reversed(range(c.layers)):
         a = k["As"][l]
         da = dh * gelu_grad(a) if l < c.layers - 1 else dh
@@ -163,16 +160,17 @@ def loss_grad(p: np.ndarray, x: np.ndarray, target: np.ndarray, c: Config, rec_x
 
 
 def build_inputs(materials, src, idx, c: Config, sigma_cells: float):
-    """Network input of se2nn_build_inputs: materials [N, ny, nx, 3], src [N, 2] (cells)."""
+    """Network input of se2nn_build_inputs: materials [N, ny, nx, 3] (row up from the bottom),
+    src [N, 2] (cells, y up from the bottom); network row 0 is the top surface."""
     B = len(idx)
     x = np.zeros((B, c.ny, c.nx, c.cin))
     cy, cx = np.meshgrid(np.arange(c.ny) + 0.5, np.arange(c.nx) + 0.5, indexing="ij")
     for b, s in enumerate(idx):
-        mt = materials[s]
+        mt = materials[s][::-1]
         x[b, :, :, 0] = (mt[..., 0] - 5000.0) / 1500.0
         x[b, :, :, 1] = (mt[..., 1] - 2800.0) / 800.0
         x[b, :, :, 2] = (mt[..., 2] - 2500.0) / 500.0
-        x[b, :, :, 3] = np.exp(-((cx - src[s][0]) ** 2 + (cy - src[s][1]) ** 2) / (2.0 * sigma_cells ** 2))
+        x[b, :, :, 3] = np.exp(-((cx - src[s][0]) ** 2 + (cy - (c.ny - src[s][1])) ** 2) / (2.0 * sigma_cells ** 2))
         x[b, :, :, 4] = (2.0 * np.floor(cx) + 1.0) / c.nx - 1.0
         x[b, :, :, 5] = (2.0 * np.floor(cy) + 1.0) / c.ny - 1.0
     return x

@@ -111,56 +111,29 @@ __global__ void k_sum_parts(const float *partial, int nparts, long n, float *out
   }
 }
 
-// mean over cells: partial sums of H[b][pix][w] over pixel chunks, then G[b][w] (bf16)
-__global__ void k_pool_partial(const bf16 *H, int npix, int w, int chunk, float *partial)
+// D0[((b*nrec + r)*ny + row)] = H[b][row][rec_x[r]][0:w]: every row of each receiver's column
+__global__ void k_decoder_gather(const bf16 *H, const int *rec_x, int B, int nrec, int ny, int nx, int w, bf16 *D0)
 {
-  // block (chunk index, b); thread c < w
-  const int b = blockIdx.y, k = blockIdx.x;
-  const int p0 = k * chunk, p1 = (p0 + chunk < npix) ? p0 + chunk : npix;
-  for (int c = threadIdx.x; c < w; c += blockDim.x) {
-    float s = 0.f;
-    for (int p = p0; p < p1; p++) s += __bfloat162float(H[((long)b * npix + p) * w + c]);
-    partial[((long)b * gridDim.x + k) * w + c] = s;
-  }
-}
-
-// D0[b*nrec + r] = [H[b][ny-1][rec_x[r]][0:w], mean_b[0:w]]
-__global__ void k_decoder_gather(const bf16 *H, const float *pool_partial, int nchunks, const int *rec_x, int B,
-                                 int nrec, int ny, int nx, int w, bf16 *D0)
-{
-  const long n = (long)B * nrec * 2 * w;
-  const float inv = 1.0f / (float)(ny * nx);
+  const long n = (long)B * nrec * ny * w;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const int c = (int)(i % (2 * w));
-    const long row = i / (2 * w);
-    const int r = (int)(row % nrec), b = (int)(row / nrec);
-    float v;
-    if (c < w) {
-      v = __bfloat162float(H[(((long)b * ny + (ny - 1)) * nx + rec_x[r]) * w + c]);
-    } else {
-      float s = 0.f;
-      for (int k = 0; k < nchunks; k++) s += pool_partial[((long)b * nchunks + k) * w + (c - w)];
-      v = s * inv;
-    }
-    D0[i] = __float2bfloat16(v);
+    const int c = (int)(i % w);
+    const long q = i / w;
+    const int row = (int)(q % ny), r = (int)((q / ny) % nrec), b = (int)(q / ((long)ny * nrec));
+    D0[i] = H[(((long)b * ny + row) * nx + rec_x[r]) * w + c];
   }
 }
 
-// dH[b][y][x][c] from dD0: mean-pool part everywhere, gathered part at the receivers' cells
+// dH[b][row][x][c] = sum over receivers r in column x of dD0[((b*nrec + r)*ny + row)][c]
 __global__ void k_decoder_scatter(const bf16 *dD0, const int *rec_x, int B, int nrec, int ny, int nx, int w, bf16 *dH)
 {
   const long n = (long)B * ny * nx * w;
-  const float inv = 1.0f / (float)(ny * nx);
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const int c = (int)(i % w);
     const long pix = i / w;
-    const int x = (int)(pix % nx), y = (int)((pix / nx) % ny), b = (int)(pix / ((long)nx * ny));
-    float g = 0.f;
-    for (int r = 0; r < nrec; r++) g += __bfloat162float(dD0[((long)b * nrec + r) * 2 * w + w + c]);
-    float v = g * inv;
-    if (y == ny - 1)
-      for (int r = 0; r < nrec; r++)
-        if (rec_x[r] == x) v += __bfloat162float(dD0[((long)b * nrec + r) * 2 * w + c]);
+    const int x = (int)(pix % nx), row = (int)((pix / nx) % ny), b = (int)(pix / ((long)nx * ny));
+    float v = 0.f;
+    for (int r = 0; r < nrec; r++)
+      if (rec_x[r] == x) v += __bfloat162float(dD0[(((long)b * nrec + r) * ny + row) * w + c]);
     dH[i] = __float2bfloat16(v);
   }
 }
@@ -207,8 +180,9 @@ __global__ void k_build_inputs(const float *mat, const float *src, const int *id
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const int cx = (int)(i % nx), cy = (int)((i / nx) % ny), b = (int)(i / ((long)nx * ny));
     const long s = idx[b];
-    const float *mm = mat + ((s * ny + cy) * nx + cx) * 3;
-    const float dx = (cx + 0.5f) - src[2 * s], dy = (cy + 0.5f) - src[2 * s + 1];
+    // network row cy counts down from the top surface: material row ny - 1 - cy, source row ny - y
+    const float *mm = mat + ((s * ny + (ny - 1 - cy)) * nx + cx) * 3;
+    const float dx = (cx + 0.5f) - src[2 * s], dy = (cy + 0.5f) - ((float)ny - src[2 * s + 1]);
     float ch[6];
     ch[0] = (mm[0] - 5000.f) * (1.f / 1500.f);   // vp
     ch[1] = (mm[1] - 2800.f) * (1.f / 800.f);    // vs
@@ -251,10 +225,10 @@ struct se2nn {
   bf16 *S = nullptr, *Xf = nullptr, *Z = nullptr, *Yp = nullptr, *Y = nullptr, *Yy = nullptr, *dZp = nullptr;
   bf16 *D0 = nullptr, *D1pre = nullptr, *D1 = nullptr, *dpred = nullptr;
   bf16 *dHa = nullptr, *dHb = nullptr, *dA = nullptr, *dD1 = nullptr, *dD0 = nullptr;
-  float *out = nullptr, *pool = nullptr, *partial = nullptr, *dblk = nullptr;
+  float *out = nullptr, *partial = nullptr, *dblk = nullptr;
   double *lpart = nullptr;
   long partial_n = 0;
-  int pool_chunks = 0, split = 1;
+  int split = 1, nsub = 1;
   cudaStream_t stream = nullptr;
   std::vector<void *> allocs;
   char err[512] = {0};
@@ -354,10 +328,10 @@ int build_dft(se2nn *h)
 // refresh the BF16 operand copies from the FP32 master parameters
 int refresh_bf16(se2nn *h)
 {
-  const int w = h->w, cin = h->c.cin, hid = h->c.hidden, nout = h->c.nout;
+  const int w = h->w, cin = h->c.cin, hid = h->c.hidden, ns = h->nsub;
   k_f32_to_bf16<<<nblk((long)cin * w), EW, 0, h->stream>>>(h->params + h->oW0, h->W0b, (long)cin * w);
-  k_f32_to_bf16<<<nblk((long)2 * w * hid), EW, 0, h->stream>>>(h->params + h->oW1, h->W1b, (long)2 * w * hid);
-  k_f32_to_bf16<<<nblk((long)hid * nout), EW, 0, h->stream>>>(h->params + h->oW2, h->W2b, (long)hid * nout);
+  k_f32_to_bf16<<<nblk((long)w * hid), EW, 0, h->stream>>>(h->params + h->oW1, h->W1b, (long)w * hid);
+  k_f32_to_bf16<<<nblk((long)hid * ns), EW, 0, h->stream>>>(h->params + h->oW2, h->W2b, (long)hid * ns);
   for (int l = 0; l < h->L; l++) {
     k_f32_to_bf16<<<nblk((long)w * w), EW, 0, h->stream>>>(h->params + h->oW[l], h->Wb[l], (long)w * w);
     const long nb = (long)h->nmodes * 4 * w * w;
@@ -417,6 +391,17 @@ int weight_grad(se2nn *h, const bf16 *X, int rows, const bf16 *dY, int B, float 
   return 0;
 }
 
+// out (M x N, f32) = X^T dY for X [K][M], dY [K][N] (bf16, K rows a multiple of chunk), split-K in fixed order
+int splitk_grad(se2nn *h, const bf16 *X, int M, const bf16 *dY, int N, long K, long chunk, float *out)
+{
+  const int parts = (int)(K / chunk);
+  GemmArgs g = mk(X, M, chunk * M, 1, dY, N, chunk * N, 0, M, N, (int)chunk, parts, h->partial, N, (long)M * N, 1);
+  GEMM(h, g);
+  k_sum_parts<<<nblk((long)M * N), EW, 0, h->stream>>>(h->partial, parts, (long)M * N, out);
+  NCK(h, cudaGetLastError());
+  return 0;
+}
+
 // S = spectral convolution of Hin with layer l's weights; the mode-major input is kept in Zp[l]
 int spectral_fwd(se2nn *h, int l, const bf16 *Hin, int B, bf16 *Sout)
 {
@@ -457,8 +442,8 @@ int spectral_bwd(se2nn *h, int l, const bf16 *dS, int B, bf16 *dHacc)
 
 int forward(se2nn *h, const bf16 *x, int B, float *out)
 {
-  const int w = h->w, npix = h->npix, L = h->L, nrec = h->c.nrec, hid = h->c.hidden, nout = h->c.nout;
-  const long rows = (long)B * npix;
+  const int w = h->w, L = h->L, nrec = h->c.nrec, hid = h->c.hidden;
+  const long rows = (long)B * h->npix;
   {
     GemmArgs g = mk(x, h->c.cin, 0, 0, h->W0b, w, 0, 0, (int)rows, w, h->c.cin, 1, h->H[0], w, 0, 0);
     g.bias = h->params + h->ob0;
@@ -474,16 +459,15 @@ int forward(se2nn *h, const bf16 *x, int B, float *out)
     GEMM(h, g);
   }
   const bf16 *HL = h->H[L];
-  k_pool_partial<<<dim3(h->pool_chunks, B), 64, 0, h->stream>>>(HL, npix, w, (npix + h->pool_chunks - 1) / h->pool_chunks, h->pool);
-  k_decoder_gather<<<nblk((long)B * nrec * 2 * w), EW, 0, h->stream>>>(HL, h->pool, h->pool_chunks, h->rec_x, B, nrec,
-                                                                       h->c.ny, h->c.nx, w, h->D0);
+  const long drows = (long)B * nrec * h->c.ny;
+  k_decoder_gather<<<nblk(drows * w), EW, 0, h->stream>>>(HL, h->rec_x, B, nrec, h->c.ny, h->c.nx, w, h->D0);
   {
-    GemmArgs g = mk(h->D0, 2 * w, 0, 0, h->W1b, hid, 0, 0, B * nrec, hid, 2 * w, 1, h->D1, hid, 0, 0);
+    GemmArgs g = mk(h->D0, w, 0, 0, h->W1b, hid, 0, 0, (int)drows, hid, w, 1, h->D1, hid, 0, 0);
     g.bias = h->params + h->oc1; g.act = 1; g.aux = h->D1pre; g.ldaux = hid;
     GEMM(h, g);
   }
   {
-    GemmArgs g = mk(h->D1, hid, 0, 0, h->W2b, nout, 0, 0, B * nrec, nout, hid, 1, out, nout, 0, 1);
+    GemmArgs g = mk(h->D1, hid, 0, 0, h->W2b, h->nsub, 0, 0, (int)drows, h->nsub, hid, 1, out, h->nsub, 0, 1);
     g.bias = h->params + h->oc2;
     GEMM(h, g);
   }
@@ -493,17 +477,17 @@ int forward(se2nn *h, const bf16 *x, int B, float *out)
 
 int backward(se2nn *h, const bf16 *x, int B)
 {
-  const int w = h->w, npix = h->npix, L = h->L, nrec = h->c.nrec, hid = h->c.hidden, nout = h->c.nout;
-  const long rows = (long)B * npix, drows = (long)B * nrec;
+  const int w = h->w, npix = h->npix, L = h->L, nrec = h->c.nrec, hid = h->c.hidden, ns = h->nsub;
+  const long rows = (long)B * npix, drows = (long)B * nrec * h->c.ny;
   int rc;
-  // decoder
-  GEMM(h, mk(h->D1, hid, 0, 1, h->dpred, nout, 0, 0, hid, nout, (int)drows, 1, h->grads + h->oW2, nout, 0, 1));
-  if ((rc = colsum(h, h->dpred, drows, nout, 64, h->grads + h->oc2))) return rc;
-  GEMM(h, mk(h->dpred, nout, 0, 0, h->W2b, nout, 0, 1, (int)drows, hid, nout, 1, h->dD1, hid, 0, 0));
+  // decoder (pointwise MLP over the receivers' columns); drows is a multiple of ny
+  if ((rc = splitk_grad(h, h->D1, hid, h->dpred, ns, drows, h->c.ny, h->grads + h->oW2))) return rc;
+  if ((rc = colsum(h, h->dpred, drows, ns, 256, h->grads + h->oc2))) return rc;
+  GEMM(h, mk(h->dpred, ns, 0, 0, h->W2b, ns, 0, 1, (int)drows, hid, ns, 1, h->dD1, hid, 0, 0));
   k_gelu_bwd<<<nblk(drows * hid), EW, 0, h->stream>>>(h->dD1, h->D1pre, h->dD1, drows * hid);
-  GEMM(h, mk(h->D0, 2 * w, 0, 1, h->dD1, hid, 0, 0, 2 * w, hid, (int)drows, 1, h->grads + h->oW1, hid, 0, 1));
-  if ((rc = colsum(h, h->dD1, drows, hid, 64, h->grads + h->oc1))) return rc;
-  GEMM(h, mk(h->dD1, hid, 0, 0, h->W1b, hid, 0, 1, (int)drows, 2 * w, hid, 1, h->dD0, 2 * w, 0, 0));
+  if ((rc = splitk_grad(h, h->D0, w, h->dD1, hid, drows, h->c.ny, h->grads + h->oW1))) return rc;
+  if ((rc = colsum(h, h->dD1, drows, hid, 256, h->grads + h->oc1))) return rc;
+  GEMM(h, mk(h->dD1, hid, 0, 0, h->W1b, hid, 0, 1, (int)drows, w, hid, 1, h->dD0, w, 0, 0));
   k_decoder_scatter<<<nblk(rows * w), EW, 0, h->stream>>>(h->dD0, h->rec_x, B, nrec, h->c.ny, h->c.nx, w, h->dHa);
   // Fourier layers, last to first: dHa holds dL/dH[l+1]
   for (int l = L - 1; l >= 0; l--) {
@@ -545,7 +529,7 @@ extern "C" int se2nn_create(const se2nn_config *cfg, unsigned long long seed, se
   *out = nullptr;
   const se2nn_config c = *cfg;
   if (c.ny < 2 || c.nx < 2 || c.cin < 16 || c.cin % 16 || c.width < 16 || c.width % 16 || c.modes < 1 ||
-      2 * c.modes > c.ny || 2 * c.modes > c.nx || c.layers < 1 || c.nrec < 1 || c.nout < 8 || c.nout % 8 ||
+      2 * c.modes > c.ny || 2 * c.modes > c.nx || c.layers < 1 || c.nrec < 1 || c.nout < c.ny || c.nout % c.ny ||
       c.hidden < 16 || c.hidden % 16 || c.max_batch < 1)
     return nfail(nullptr, -1, "invalid network configuration");
   if ((long)c.max_batch * c.ny > 65535 || 2L * c.modes * c.modes > 65535 ||
@@ -566,13 +550,13 @@ extern "C" int se2nn_create(const se2nn_config *cfg, unsigned long long seed, se
     h->oW.push_back(o); o += (long)w * w;
     h->ob.push_back(o); o += w;
   }
-  h->oW1 = o; o += 2L * w * c.hidden;
+  h->nsub = c.nout / c.ny;
+  h->oW1 = o; o += (long)w * c.hidden;
   h->oc1 = o; o += c.hidden;
-  h->oW2 = o; o += (long)c.hidden * c.nout;
-  h->oc2 = o; o += c.nout;
+  h->oW2 = o; o += (long)c.hidden * h->nsub;
+  h->oc2 = o; o += h->nsub;
   h->P = o;
   h->split = (npix % 8 == 0) ? 8 : (npix % 4 == 0) ? 4 : (npix % 2 == 0) ? 2 : 1;
-  h->pool_chunks = (int)std::min<long>(32, npix);
   int rc = 0;
 #define TRY(x) do { if ((rc = (x)) != 0) { snprintf(g_nn_create_err, sizeof(g_nn_create_err), "%s", h->err); se2nn_destroy(h); return rc; } } while (0)
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -585,8 +569,8 @@ extern "C" int se2nn_create(const se2nn_config *cfg, unsigned long long seed, se
   TRY(nalloc(h, &h->adam_m, h->P));
   TRY(nalloc(h, &h->adam_v, h->P));
   TRY(nalloc(h, &h->W0b, (size_t)c.cin * w));
-  TRY(nalloc(h, &h->W1b, (size_t)2 * w * c.hidden));
-  TRY(nalloc(h, &h->W2b, (size_t)c.hidden * c.nout));
+  TRY(nalloc(h, &h->W1b, (size_t)w * c.hidden));
+  TRY(nalloc(h, &h->W2b, (size_t)c.hidden * h->nsub));
   h->Wb.assign(L, nullptr); h->Wblk.assign(L, nullptr); h->Zp.assign(L, nullptr);
   h->H.assign(L + 1, nullptr); h->Apre.assign(L > 1 ? L - 1 : 0, nullptr);
   for (int l = 0; l < L; l++) {
@@ -607,22 +591,22 @@ extern "C" int se2nn_create(const se2nn_config *cfg, unsigned long long seed, se
   TRY(nalloc(h, &h->Yy, (size_t)Bm * 2 * c.ny * h->m * w));
   TRY(nalloc(h, &h->Yp, (size_t)nm * Bm * 2 * w));
   TRY(nalloc(h, &h->dZp, (size_t)nm * Bm * 2 * w));
-  const size_t drows = (size_t)Bm * c.nrec;
-  TRY(nalloc(h, &h->D0, drows * 2 * w));
-  TRY(nalloc(h, &h->dD0, drows * 2 * w));
+  const size_t drows = (size_t)Bm * c.nrec * c.ny;
+  TRY(nalloc(h, &h->D0, drows * w));
+  TRY(nalloc(h, &h->dD0, drows * w));
   TRY(nalloc(h, &h->D1pre, drows * c.hidden));
   TRY(nalloc(h, &h->D1, drows * c.hidden));
   TRY(nalloc(h, &h->dD1, drows * c.hidden));
-  TRY(nalloc(h, &h->out, drows * c.nout));
-  TRY(nalloc(h, &h->dpred, drows * c.nout));
-  TRY(nalloc(h, &h->pool, (size_t)Bm * h->pool_chunks * w));
+  TRY(nalloc(h, &h->out, drows * h->nsub));
+  TRY(nalloc(h, &h->dpred, drows * h->nsub));
   TRY(nalloc(h, &h->dblk, (size_t)nm * 4 * w * w));
   TRY(nalloc(h, &h->lpart, 1024));
   TRY(nalloc(h, &h->rec_x, (size_t)c.nrec));
   {
     const long wg = (long)Bm * h->split * (long)w * std::max(w, c.cin);
     const long cs1 = (((long)Bm * npix + 1023) / 1024) * w;
-    const long cs2 = (((long)drows + 63) / 64) * std::max(c.nout, c.hidden);
+    const long cs2 = std::max((long)Bm * c.nrec * (long)c.hidden * std::max(w, h->nsub),
+                              (((long)drows + 255) / 256) * std::max(h->nsub, c.hidden));
     h->partial_n = std::max(wg, std::max(cs1, cs2));
     TRY(nalloc(h, &h->partial, (size_t)h->partial_n));
   }
@@ -637,8 +621,8 @@ extern "C" int se2nn_create(const se2nn_config *cfg, unsigned long long seed, se
       for (long i = 0; i < nm * w * w; i++) p[h->oWim[l] + i] = uniform_pm(&s, 1.0f / (float)w);
       for (long i = 0; i < (long)w * w; i++) p[h->oW[l] + i] = uniform_pm(&s, 1.0f / sqrtf((float)w));
     }
-    for (long i = 0; i < 2L * w * c.hidden; i++) p[h->oW1 + i] = uniform_pm(&s, 1.0f / sqrtf(2.0f * w));
-    for (long i = 0; i < (long)c.hidden * c.nout; i++) p[h->oW2 + i] = uniform_pm(&s, 1.0f / sqrtf((float)c.hidden));
+    for (long i = 0; i < (long)w * c.hidden; i++) p[h->oW1 + i] = uniform_pm(&s, 1.0f / sqrtf((float)w));
+    for (long i = 0; i < (long)c.hidden * h->nsub; i++) p[h->oW2 + i] = uniform_pm(&s, 1.0f / sqrtf((float)c.hidden));
     if (cudaMemcpy(h->params, p.data(), h->P * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemset(h->grads, 0, h->P * 4) != cudaSuccess || cudaMemset(h->adam_m, 0, h->P * 4) != cudaSuccess ||
         cudaMemset(h->adam_v, 0, h->P * 4) != cudaSuccess) {

@@ -33,7 +33,7 @@ class CConfig(C.Structure):
 @dataclasses.dataclass
 class Config:
     """Network shape; the defaults are the 128^2, width-64, 16-mode, 4-layer operator
-    producing 16 receivers x 2 components x 1024 samples."""
+    producing 16 receivers x 128 rows x 16 values (2 components x 1024 samples)."""
     ny: int = 128
     nx: int = 128
     cin: int = 16
@@ -42,7 +42,7 @@ class Config:
     layers: int = 4
     nrec: int = 16
     nout: int = 2048
-    hidden: int = 256
+    hidden: int = 128
     max_batch: int = 32
 
     def c(self) -> CConfig:

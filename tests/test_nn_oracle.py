@@ -6,7 +6,7 @@ import pytest
 
 from oracle import nn_oracle as NO
 
-CFG = NO.Config(ny=8, nx=12, cin=16, width=4, modes=2, layers=2, nrec=3, nout=5, hidden=6, max_batch=4)
+CFG = NO.Config(ny=8, nx=12, cin=16, width=4, modes=2, layers=2, nrec=3, nout=24, hidden=6, max_batch=4)
 REC = [1, 5, 10]
 
 
@@ -22,7 +22,7 @@ def sample(c=CFG, B=2, seed=0):
 def test_layout_counts():
     lay, n = NO.layout(NO.Config())
     w, m = 64, 16
-    assert n == 16 * w + w + 4 * (2 * 2 * m * m * w * w + w * w + w) + 2 * w * 256 + 256 + 256 * 2048 + 2048
+    assert n == 16 * w + w + 4 * (2 * 2 * m * m * w * w + w * w + w) + w * 128 + 128 + 128 * 16 + 16
     p = np.arange(n, dtype=np.float64)
     assert np.array_equal(NO.pack(NO.unpack(p, NO.Config()), NO.Config()), p)
 
@@ -61,10 +61,9 @@ def torch_forward(p, x, c, rec_x):
         S = torch.fft.irfft2(of, s=(c.ny, c.nx), dim=(1, 2))
         a = S + h @ P[f"W{l}"] + P[f"b{l}"]
         h = torch.nn.functional.gelu(a) if l < c.layers - 1 else a
-    G = h.mean(dim=(1, 2))
-    R = h[:, c.ny - 1, list(rec_x), :]
-    D0 = torch.cat([R, G[:, None, :].expand_as(R)], dim=2)
+    D0 = h[:, :, list(rec_x), :].permute(0, 2, 1, 3)
     out = torch.nn.functional.gelu(D0 @ P["Wdec1"] + P["cdec1"]) @ P["Wdec2"] + P["cdec2"]
+    out = out.reshape(x.shape[0], len(rec_x), -1)
     return out, P
 
 

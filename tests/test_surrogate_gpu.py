@@ -1,0 +1,46 @@
+"""Surrogate pipeline pieces that need the GPU: solver traces of mirrored
+problems (the augmentation's premise) and a short end-to-end train/predict."""
+import numpy as np
+import pytest
+
+from se2dr_fork_gb300 import spec as S
+from se2dr_fork_gb300 import surrogate as SU
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _libs(gpu_lib, nn_lib):
+    return gpu_lib, nn_lib
+
+
+def mirror_spec(sp: S.Spec) -> S.Spec:
+    flip = lambda a: np.ascontiguousarray(np.asarray(a).reshape(sp.my, sp.mx)[:, ::-1].reshape(-1))
+    src = sp.sources[0]
+    Lx = sp.mx * SU.CELL
+    return sp.replace(cell_vp=flip(sp.cell_vp), cell_vs=flip(sp.cell_vs), cell_rho=flip(sp.cell_rho),
+                      sources=[S.Source(Lx - src.x, src.y, src.moment, src.stf, src.par)])
+
+
+def test_mirrored_problem_gives_mirrored_traces(monkeypatch):
+    monkeypatch.setattr(SU, "NSTEPS", 1024)
+    monkeypatch.setattr(SU, "NSAMP", 256)
+    sp = SU.draw_spec(7, 3).replace(nt=1024)
+    traces, _ = SU.solve([sp, mirror_spec(sp)], chunk=2)
+    a = traces[0].reshape(16, 2, 256)
+    b = traces[1].reshape(16, 2, 256)
+    scale = np.abs(a).max()
+    assert scale > 0
+    assert np.max(np.abs(b[::-1, 0] + a[:, 0])) < 1e-4 * scale
+    assert np.max(np.abs(b[::-1, 1] - a[:, 1])) < 1e-4 * scale
+
+
+def test_short_training_run_fits_and_predicts():
+    ds = SU.generate(11, 64)
+    data = SU.DeviceData(ds, augment=True)
+    assert data.n == 128
+    net, st = SU.train(data, np.arange(data.n), SU.receiver_cells(ds.specs[0]), seed=0, epochs=6, batch=32, lr=2e-3)
+    assert st["loss"][-1] < st["loss"][0]
+    preds = SU.predict([net], data, np.arange(8))
+    assert preds.shape == (1, 8, 16, 2048) and np.all(np.isfinite(preds))
