@@ -120,6 +120,18 @@ int se2gpu_device_fields(const se2gpu_solver *h, void **u, void **v, void **a);
 int se2gpu_tile_configs(const se2gpu_solver *h, int *edge, int *threads, int max_configs);
 int se2gpu_set_tile_config(se2gpu_solver *h, int config);
 
+/* ---- Checkpoint / resume (no counterpart in the reference, which restarts from
+   t = 0).  The checkpoint holds the handle's whole evolving state: the fields
+   in the handle's precision (FP32 modes: leapfrog state with its Kahan terms),
+   the acceleration of the last step, and the pending receiver row, so a run
+   resumed from it is bit-identical to the uninterrupted run.  Buffered trace
+   rows are not part of it: fetch them with se2gpu_traces first (saving with
+   rows buffered fails with SE2GPU_ERR_STATE).  Load into a handle created
+   from the same problem and precision (checked against the header). */
+long se2gpu_checkpoint_size(const se2gpu_solver *h);
+int  se2gpu_checkpoint_save(se2gpu_solver *h, void *buf, long bytes);
+int  se2gpu_checkpoint_load(se2gpu_solver *h, const void *buf, long bytes);
+
 /* ---- Batched ensemble.  No counterpart in the reference, which runs one shot
    per process (se2wave.c main): many independent problems ("shots") of any
    mesh size and degree advanced in lock-step on one GPU, FP32 precisions only.

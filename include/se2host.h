@@ -40,6 +40,16 @@ typedef struct se2_spec {
   const double *stf_par;         /* nsrc*3 */
   int nrec;
   const double *rec_xy;          /* nrec*2 */
+  /* perturb != 0 (and no cell arrays): SpecFECtxSetPerturbedMaterialProperties_Velocity
+     (1177-1236): per cell, uniform in [vp - dvp, vp + dvp] etc. from PETSc's RAND48
+     (drand48 seeded 1, 2, 3 for vp, vs, rho) */
+  int perturb;
+  double dvp, dvs, drho;
+  /* source representation: < 0 SeismicSourceCreate's nearest GLL point (the demo's); 0 pointwise,
+     2 cubic-spline kernel of radius sm_h (<= 0: the reference's default), 3 P0
+     (ElastoDynamicsSetSourceImplementation / -source_impl, 2202-2266) */
+  int src_impl;
+  double sm_h;
 } se2_spec;
 
 /* Everything the device needs, FP64, owned by the library. */
@@ -69,6 +79,10 @@ typedef struct se2_setup {
   int nrec;
   double *rec_xy;
   int *rec_node, *rec_elem, *rec_gll; /* nearest GLL node (RecordUVA_MultipleStations_NearestGLL_MPI 2700-2810) */
+  /* source entries: nsrc entries (element + element values + STF), each belonging to one of the
+     nsrc_phys sources of the spec (src_owner); one entry per source unless src_impl >= 0 */
+  int nsrc_phys;
+  int *src_owner;
 } se2_setup;
 
 const char *se2_host_last_error(void);
@@ -127,6 +141,20 @@ typedef struct se2_shot_draw {
 int se2_shot_draw_params(unsigned long long seed, long index, int kind, se2_shot_draw *out);
 /* the drawn materials on the mx*my cell grid (row-major, x fastest), at cell centres */
 int se2_shot_materials(const se2_shot_draw *d, double *vp, double *vs, double *rho);
+
+/* Snapshot of nodal fields (the VecView to a PetscViewerVTK of se2wave.c:4606-4610,
+   4764-4770, 4785-4789): a VTK XML StructuredGrid file over the GLL nodes
+   (points x, y, 0), one Float64 scalar array per component named <name>_x and
+   <name>_y (the Vec names and DMDA field names of the reference), raw appended
+   data with UInt64 size headers.  vecs[v] are interleaved [node][component]. */
+int se2_write_vts(const se2_setup *s, const char *path, int nvec, const char *const *names, const double *const *vecs);
+
+/* Assembled source vector g (2*nnodes, interleaved) of one moment source M = [M00 M01 M10 M11]
+   at xy, in one of the reference's alternative representations (ElastoDynamicsSourceSetup,
+   2232-2266): 0 pointwise at the exact reference coordinates (1716-1923), 2 cubic-spline
+   smoothed Dirac with radius kernel_h (<= 0: the reference's default; -sm_h, 1925-2057),
+   3 P0 cell average (2059-2200). */
+int se2_source_vector(const se2_setup *s, int impl, double kernel_h, const double xy[2], const double M[4], double *g);
 
 #ifdef __cplusplus
 }

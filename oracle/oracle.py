@@ -31,7 +31,8 @@ class _CSpec(C.Structure):
                 ("cfl", C.c_double), ("dt", C.c_double), ("tmax", C.c_double),
                 ("nt", C.c_int), ("nearest_internal_gll", C.c_int),
                 ("nsrc", C.c_int), ("src_xy", _dp), ("src_m", _dp), ("stf_type", _ip), ("stf_par", _dp),
-                ("nrec", C.c_int), ("rec_xy", _dp)]
+                ("nrec", C.c_int), ("rec_xy", _dp),
+                ("perturb", C.c_int), ("dvp", C.c_double), ("dvs", C.c_double), ("drho", C.c_double)]
 
 
 def build(quiet: bool = True) -> str:
@@ -99,6 +100,9 @@ class _SpecHolder:
         cs.src_xy, cs.src_m, cs.stf_type, cs.stf_par = _ptr(sxy), _ptr(sm), _ptr(st, _ip), _ptr(sp)
         cs.nrec = len(spec.receivers)
         cs.rec_xy = _ptr(rxy)
+        if spec.perturb is not None:
+            cs.perturb = 1
+            cs.dvp, cs.dvs, cs.drho = spec.perturb
         self.cs = cs
 
 
@@ -192,6 +196,25 @@ def build_ref(refdir: str = "/root/reference") -> bool:
         return False
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFDIR={refdir}"], check=True, stdout=subprocess.DEVNULL)
     return True
+
+
+def ref_source_vector(spec, impl: int, extra_args=()) -> np.ndarray:
+    """The reference's assembled source vector of spec's first source by implementation
+    impl (0 pointwise, 2 cubic-spline kernel, 3 P0); extra_args e.g. ["-sm_h", "40"]."""
+    with tempfile.TemporaryDirectory() as d:
+        sfile = os.path.join(d, "spec.txt")
+        cells = spec.cell_arrays()
+        cell_file = None
+        if cells is not None:
+            cell_file = os.path.join(d, "cells.bin")
+            np.concatenate(cells).astype(np.float64).tofile(cell_file)
+        with open(sfile, "w") as f:
+            f.write(spec.to_text(cell_file))
+        r = subprocess.run([REF_DRIVER, "srcvec", sfile, str(impl), d, *extra_args], cwd=d, capture_output=True,
+                           text=True)
+        if r.returncode != 0:
+            raise RuntimeError(r.stderr[-2000:] + r.stdout[-2000:])
+        return np.fromfile(os.path.join(d, "g.bin"), dtype=np.float64)
 
 
 def ref_run(spec, extra_args=(), force_u: Optional[np.ndarray] = None) -> dict:

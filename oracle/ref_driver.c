@@ -87,6 +87,8 @@ typedef struct {
   double stf_par[3 * MAXS];
   int nrec;
   double rec_xy[2 * MAXR];
+  int perturb;
+  double dvp, dvs, drho;
 } Spec;
 
 static int read_spec(const char *fname, Spec *sp)
@@ -110,6 +112,7 @@ static int read_spec(const char *fname, Spec *sp)
     else if (!strcmp(key, "rho")) fscanf(f, "%lf", &sp->rho);
     else if (!strcmp(key, "cell_file")) fscanf(f, "%1023s", sp->cell_file);
     else if (!strcmp(key, "cfl")) fscanf(f, "%lf", &sp->cfl);
+    else if (!strcmp(key, "perturb")) { sp->perturb = 1; fscanf(f, "%lf %lf %lf", &sp->dvp, &sp->dvs, &sp->drho); }
     else if (!strcmp(key, "dt")) fscanf(f, "%lf", &sp->dt);
     else if (!strcmp(key, "tmax")) fscanf(f, "%lf", &sp->tmax);
     else if (!strcmp(key, "nt")) fscanf(f, "%d", &sp->nt);
@@ -171,6 +174,8 @@ static PetscErrorCode setup_ctx(const Spec *sp, SpecFECtx *_ctx)
       ctx->cell_data[e].rho = rho;
     }
     free(buf);
+  } else if (sp->perturb) {
+    ierr = SpecFECtxSetPerturbedMaterialProperties_Velocity(ctx, sp->vp, sp->dvp, sp->vs, sp->dvs, sp->rho, sp->drho); CHKERRQ(ierr);
   } else {
     ierr = SpecFECtxSetConstantMaterialProperties_Velocity(ctx, sp->vp, sp->vs, sp->rho); CHKERRQ(ierr);
   }
@@ -350,6 +355,27 @@ static PetscErrorCode force(const Spec *sp, const char *ufile, const char *outdi
   return 0;
 }
 
+/* assembled source vector of the spec's first source by one of the reference's
+   alternative implementations (ElastoDynamicsSourceSetup's switch, 2244-2263) */
+static PetscErrorCode srcvec(const Spec *sp, int impl, const char *outdir)
+{
+  PetscErrorCode ierr;
+  SpecFECtx ctx;
+  Vec g;
+  PetscReal xs[2], m[4];
+  int i;
+  ierr = setup_ctx(sp, &ctx); CHKERRQ(ierr);
+  ierr = DMCreateGlobalVector(ctx->dm, &g); CHKERRQ(ierr);
+  xs[0] = sp->src_xy[0]; xs[1] = sp->src_xy[1];
+  for (i = 0; i < 4; i++) m[i] = sp->src_m[i];
+  if (impl == 0) { ierr = AssembleLinearForm_ElastoDynamicsMomentDirac2d(ctx, 1, xs, m, g); CHKERRQ(ierr); }
+  else if (impl == 2) { ierr = AssembleLinearForm_ElastoDynamicsMomentDirac2d_Kernel_CSpline(ctx, 1, xs, m, g); CHKERRQ(ierr); }
+  else if (impl == 3) { ierr = AssembleLinearForm_ElastoDynamicsMomentDirac2d_P0(ctx, 1, xs, m, g); CHKERRQ(ierr); }
+  else SETERRQ(PETSC_COMM_SELF, PETSC_ERR_USER, "implementation 0, 2 or 3");
+  dump(outdir, "g.bin", g->array, sizeof(double) * g->n);
+  return 0;
+}
+
 static PetscErrorCode stf_table(int argc, char **argv)
 {
   SeismicSTF stf;
@@ -401,6 +427,11 @@ int main(int argc, char **argv)
     return force(&sp, argv[3], argv[4]) ? 2 : 0;
   }
   if (!strcmp(argv[1], "stf") && argc >= 10) return stf_table(argc, argv) ? 2 : 0;
+  if (!strcmp(argv[1], "srcvec") && argc >= 5) {
+    PetscLiteOptionsSet(argc - 4, argv + 4);
+    if (read_spec(argv[2], &sp)) return 1;
+    return srcvec(&sp, atoi(argv[3]), argv[4]) ? 2 : 0;
+  }
   fprintf(stderr, "bad arguments\n");
   return 1;
 }

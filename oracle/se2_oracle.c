@@ -550,13 +550,31 @@ int se2o_create(const se2o_spec *sp, se2o_ctx **out)
   c->lam = (double*)malloc(sizeof(double) * c->ne);
   c->mu = (double*)malloc(sizeof(double) * c->ne);
   c->rho = (double*)malloc(sizeof(double) * c->ne);
-  for (e = 0; e < c->ne; e++) {
-    double vp = sp->cell_vp ? sp->cell_vp[e] : sp->vp;
-    double vs = sp->cell_vs ? sp->cell_vs[e] : sp->vs;
-    double rho = sp->cell_rho ? sp->cell_rho[e] : sp->rho;
-    double mu = vs * vs * rho;
-    double lambda = vp * vp * rho - 2.0 * mu;
-    c->lam[e] = lambda; c->mu[e] = mu; c->rho[e] = rho;
+  {
+    /* perturbed (1177-1236): VecSetRandom of three Vecs with RAND48 seeded 1, 2, 3 */
+    double *pv = NULL;
+    if (!sp->cell_vp && sp->perturb) {
+      const double base[3] = {sp->vp, sp->vs, sp->rho}, del[3] = {sp->dvp, sp->dvs, sp->drho};
+      int f;
+      pv = (double*)malloc(sizeof(double) * 3 * (size_t)c->ne);
+      for (f = 0; f < 3; f++) {
+        double low = base[f] - del[f], width = (base[f] + del[f]) - low;
+        unsigned long long x = ((unsigned long long)(unsigned int)(f + 1) << 16) | 0x330EULL;
+        for (e = 0; e < c->ne; e++) {
+          x = (0x5DEECE66DULL * x + 0xBULL) & 0xFFFFFFFFFFFFULL;
+          pv[f * c->ne + e] = width * ((double)x / 281474976710656.0) + low;
+        }
+      }
+    }
+    for (e = 0; e < c->ne; e++) {
+      double vp = pv ? pv[e] : sp->cell_vp ? sp->cell_vp[e] : sp->vp;
+      double vs = pv ? pv[c->ne + e] : sp->cell_vs ? sp->cell_vs[e] : sp->vs;
+      double rho = pv ? pv[2 * c->ne + e] : sp->cell_rho ? sp->cell_rho[e] : sp->rho;
+      double mu = vs * vs * rho;
+      double lambda = vp * vp * rho - 2.0 * mu;
+      c->lam[e] = lambda; c->mu[e] = mu; c->rho[e] = rho;
+    }
+    free(pv);
   }
   /* vectors */
   c->u = (double*)calloc((size_t)c->ndof, sizeof(double));

@@ -32,6 +32,8 @@ typedef struct {
   const double *stf_par;         /* nsrc*3 */
   int nrec;
   const double *rec_xy;          /* nrec*2 */
+  int perturb;                   /* SpecFECtxSetPerturbedMaterialProperties_Velocity (1177-1236) */
+  double dvp, dvs, drho;
 } se2o_spec;
 
 typedef struct se2o_ctx se2o_ctx;

@@ -258,6 +258,14 @@ static uint64_t splitmix64(uint64_t *st)
   return z ^ (z >> 31);
 }
 
+/* POSIX rand48 (drand48 after srand48): X' = (0x5DEECE66D X + 0xB) mod 2^48, value X' / 2^48 */
+static uint64_t rand48_seeded(long seed) { return ((uint64_t)(uint32_t)seed << 16) | 0x330EULL; }
+static double rand48_next(uint64_t *x)
+{
+  *x = (0x5DEECE66DULL * *x + 0xBULL) & 0xFFFFFFFFFFFFULL;
+  return (double)*x * (1.0 / 281474976710656.0);
+}
+
 int se2_gaussian_random_field(int mx, int my, double mean, double rel_std, double corr, unsigned long long seed,
                               double *out)
 {
@@ -395,6 +403,56 @@ int se2_shot_materials(const se2_shot_draw *d, double *vp, double *vs, double *r
 }
 
 /* ------------------------------------------------------------------ */
+/* VTS snapshots (VTK XML StructuredGrid, raw appended Float64)        */
+/* ------------------------------------------------------------------ */
+int se2_write_vts(const se2_setup *s, const char *path, int nvec, const char *const *names, const double *const *vecs)
+{
+  FILE *f;
+  const long nx = s ? s->nx_g : 0, ny = s ? s->ny_g : 0, n = nx * ny;
+  unsigned long long off = 0, nbytes;
+  long i, j;
+  int v, c;
+  if (!s || !path || nvec < 0 || (nvec > 0 && (!names || !vecs))) SE2_FAIL("bad VTS arguments");
+  f = fopen(path, "wb");
+  if (!f) SE2_FAIL("cannot open %s", path);
+  fprintf(f, "<?xml version=\"1.0\"?>\n");
+  fprintf(f, "<VTKFile type=\"StructuredGrid\" version=\"1.0\" byte_order=\"LittleEndian\" header_type=\"UInt64\">\n");
+  fprintf(f, "  <StructuredGrid WholeExtent=\"0 %ld 0 %ld 0 0\">\n", nx - 1, ny - 1);
+  fprintf(f, "    <Piece Extent=\"0 %ld 0 %ld 0 0\">\n", nx - 1, ny - 1);
+  fprintf(f, "      <Points>\n");
+  fprintf(f, "        <DataArray type=\"Float64\" Name=\"Position\" NumberOfComponents=\"3\" format=\"appended\" offset=\"%llu\" />\n", off);
+  off += 8ULL + 24ULL * (unsigned long long)n;
+  fprintf(f, "      </Points>\n");
+  fprintf(f, "      <PointData>\n");
+  for (v = 0; v < nvec; v++)
+    for (c = 0; c < 2; c++) {
+      fprintf(f, "        <DataArray type=\"Float64\" Name=\"%s%s\" NumberOfComponents=\"1\" format=\"appended\" offset=\"%llu\" />\n",
+              names[v], c ? "_y" : "_x", off);
+      off += 8ULL + 8ULL * (unsigned long long)n;
+    }
+  fprintf(f, "      </PointData>\n");
+  fprintf(f, "    </Piece>\n");
+  fprintf(f, "  </StructuredGrid>\n");
+  fprintf(f, "  <AppendedData encoding=\"raw\">\n_");
+  nbytes = 24ULL * (unsigned long long)n;
+  fwrite(&nbytes, 8, 1, f);
+  for (j = 0; j < ny; j++)
+    for (i = 0; i < nx; i++) {
+      const double p[3] = {s->xnode[i], s->ynode[j], 0.0};
+      fwrite(p, 8, 3, f);
+    }
+  nbytes = 8ULL * (unsigned long long)n;
+  for (v = 0; v < nvec; v++)
+    for (c = 0; c < 2; c++) {
+      fwrite(&nbytes, 8, 1, f);
+      for (i = 0; i < n; i++) fwrite(&vecs[v][2 * i + c], 8, 1, f);
+    }
+  fprintf(f, "\n  </AppendedData>\n</VTKFile>\n");
+  if (fclose(f) != 0) SE2_FAIL("write error on %s", path);
+  return 0;
+}
+
+/* ------------------------------------------------------------------ */
 /* set-up                                                              */
 /* ------------------------------------------------------------------ */
 void se2_setup_destroy(se2_setup *s)
@@ -403,6 +461,7 @@ void se2_setup_destroy(se2_setup *s)
   free(s->xi); free(s->w1d); free(s->wq); free(s->D); free(s->xnode); free(s->ynode);
   free(s->J00); free(s->J11); free(s->iJ00); free(s->iJ11); free(s->lambda); free(s->mu); free(s->rho);
   free(s->mass); free(s->src_elem); free(s->src_gll); free(s->src_vals); free(s->stf_type); free(s->stf_par);
+  free(s->src_owner);
   free(s->rec_xy); free(s->rec_node); free(s->rec_elem); free(s->rec_gll);
   free(s);
 }
@@ -471,6 +530,133 @@ static int locate_source(se2_setup *s, int k, const double c[2], const double M[
       s->src_vals[(size_t)k * 2 * npe + 2 * q + 1] = (M[2] * gx + M[3] * gy);
     }
   return 0;
+}
+
+/* ---- alternative moment-source representations (ElastoDynamicsSourceSetup, 2232-2266):
+   the assembled source vector g (2 * nnodes, interleaved) of one moment source */
+static int source_cell(const se2_setup *s, const double xy[2], int *ii, int *jj, double *dx, double *dy)
+{
+  *dx = (s->gmax[0] - s->gmin[0]) / ((double)s->mx);
+  *dy = (s->gmax[1] - s->gmin[1]) / ((double)s->my);
+  *ii = (int)((xy[0] - s->gmin[0]) / *dx);
+  *jj = (int)((xy[1] - s->gmin[1]) / *dy);
+  if (*ii == s->mx) (*ii)--;
+  if (*jj == s->my) (*jj)--;
+  if (*ii < 0) SE2_FAIL("source: x < gmin[0]");
+  if (*jj < 0) SE2_FAIL("source: y < gmin[1]");
+  if (*ii >= s->mx || *jj >= s->my) SE2_FAIL("source outside the domain");
+  return 0;
+}
+
+/* dN/dx, dN/dy (npe each) at reference point xi of element (ei, ej):
+   TabulateBasisDerivativesAtPointTensorProduct2d + ElementEvaluateDerivatives_CellWiseConstant2d */
+static int point_derivs(const se2_setup *s, int ei, int ej, const double xi[2], double *gx, double *gy)
+{
+  const int n1 = s->n1;
+  double dxi[17], Nxi[17], deta[17], Neta[17];
+  int a, b;
+  if (se2_basis_deriv_1d(s->p, 1, &xi[0], dxi) || se2_basis_1d(s->p, 1, &xi[0], Nxi) ||
+      se2_basis_deriv_1d(s->p, 1, &xi[1], deta) || se2_basis_1d(s->p, 1, &xi[1], Neta)) return -1;
+  for (b = 0; b < n1; b++)
+    for (a = 0; a < n1; a++) {
+      gx[a + b * n1] = s->iJ00[ei] * (dxi[a] * Neta[b]);
+      gy[a + b * n1] = s->iJ11[ej] * (Nxi[a] * deta[b]);
+    }
+  return 0;
+}
+
+int se2_source_vector(const se2_setup *s, int impl, double kernel_h, const double xy[2], const double M[4], double *g)
+{
+  const int p = s ? s->p : 0, n1 = s ? s->n1 : 0, npe = s ? s->npe : 0;
+  double gx[289], gy[289], fe[578];
+  int ii, jj, i, q, e;
+  double dx, dy;
+  if (!s || !xy || !M || !g) SE2_FAIL("null argument");
+  memset(g, 0, sizeof(double) * 2 * (size_t)s->nnodes);
+  if (impl == 0 || impl == 3) {
+    /* 0: pointwise at the source's reference coordinates (1716-1923); 3: P0, the cell centre with
+       the cell-averaged weight (2059-2200) */
+    double xi[2], detJ;
+    if (source_cell(s, xy, &ii, &jj, &dx, &dy)) return -1;
+    if (impl == 0) {
+      const double cmin0 = s->gmin[0] + ii * dx, cmin1 = s->gmin[1] + jj * dy;
+      xi[0] = 2.0 * (xy[0] - cmin0) / dx - 1.0;
+      xi[1] = 2.0 * (xy[1] - cmin1) / dy - 1.0;
+      if (fabs(xi[0]) < 1.0e-12) xi[0] = 0.0;
+      if (fabs(xi[1]) < 1.0e-12) xi[1] = 0.0;
+    } else {
+      xi[0] = 0.0;
+      xi[1] = 0.0;
+    }
+    if (point_derivs(s, ii, jj, xi, gx, gy)) return -1;
+    memset(fe, 0, sizeof(double) * 2 * npe);
+    if (impl == 0) {
+      for (i = 0; i < npe; i++) {
+        fe[2 * i] += (M[0] * gx[i] + M[1] * gy[i]);
+        fe[2 * i + 1] += (M[2] * gx[i] + M[3] * gy[i]);
+      }
+    } else {
+      detJ = s->J00[ii] * s->J11[jj];
+      for (q = 0; q < npe; q++)
+        for (i = 0; i < npe; i++) {
+          fe[2 * i] += s->wq[q] * detJ * (M[0] * gx[i] + M[1] * gy[i]) / (dx * dy);
+          fe[2 * i + 1] += s->wq[q] * detJ * (M[2] * gx[i] + M[3] * gy[i]) / (dx * dy);
+        }
+    }
+    for (i = 0; i < npe; i++) {
+      const long node = (long)(ii * p + i % n1) + (long)(jj * p + i / n1) * s->nx_g;
+      g[2 * node] += fe[2 * i];
+      g[2 * node + 1] += fe[2 * i + 1];
+    }
+    return 0;
+  }
+  if (impl == 2) {
+    /* cubic-spline smoothed Dirac over every element (1925-2057) */
+    double ds, h;
+    dx = (s->gmax[0] - s->gmin[0]) / ((double)s->mx);
+    dy = (s->gmax[1] - s->gmin[1]) / ((double)s->my);
+    ds = dx;
+    if (dy > dx) ds = dy;
+    if (kernel_h > 0.0) h = kernel_h;
+    else if (p <= 3) h = 1.5 * (0.5 * ds);
+    else h = (3.0 / (p - 2.0)) * (0.5 * ds);
+    /* basis and derivative tables at the GLL points (TabulateBasisDerivativesTensorProduct2d, 525-603) */
+    for (e = 0; e < s->mx * s->my; e++) {
+      const int ei = e % s->mx, ej = e / s->mx;
+      const double detJ = s->J00[ei] * s->J11[ej];
+      memset(fe, 0, sizeof(double) * 2 * npe);
+      for (q = 0; q < npe; q++) {
+        const int qa = q % n1, qb = q / n1;
+        const double xq0 = s->xnode[ei * p + qa], xq1 = s->ynode[ej * p + qb];
+        double sep, arg, sd;
+        /* dN/dx, dN/dy at GLL point q: the 1-D derivative matrix times exact Kronecker deltas
+           (TabulateBasisDerivativesTensorProduct2d, 525-603), scaled by the inverse Jacobian */
+        for (i = 0; i < npe; i++) {
+          const int ia = i % n1, ib = i / n1;
+          gx[i] = s->iJ00[ei] * (s->D[qa * n1 + ia] * ((qb == ib) ? 1.0 : 0.0));
+          gy[i] = s->iJ11[ej] * (((qa == ia) ? 1.0 : 0.0) * s->D[qb * n1 + ib]);
+        }
+        sep = (xq0 - xy[0]) * (xq0 - xy[0]);
+        sep += (xq1 - xy[1]) * (xq1 - xy[1]);
+        arg = sqrt(sep) / h;
+        if (arg < 1.0) sd = 0.25 * (2.0 - arg) * (2.0 - arg) * (2.0 - arg) - (1.0 - arg) * (1.0 - arg) * (1.0 - arg);
+        else if (arg < 2.0) sd = 0.25 * (2.0 - arg) * (2.0 - arg) * (2.0 - arg);
+        else sd = 0.0;
+        sd = 10.0 / (7.0 * SE2_PI) * sd * (1.0 / (h * h));
+        for (i = 0; i < npe; i++) {
+          fe[2 * i] += s->wq[q] * detJ * (M[0] * gx[i] + M[1] * gy[i]) * sd;
+          fe[2 * i + 1] += s->wq[q] * detJ * (M[2] * gx[i] + M[3] * gy[i]) * sd;
+        }
+      }
+      for (i = 0; i < npe; i++) {
+        const long node = (long)(ei * p + i % n1) + (long)(ej * p + i / n1) * s->nx_g;
+        g[2 * node] += fe[2 * i];
+        g[2 * node + 1] += fe[2 * i + 1];
+      }
+    }
+    return 0;
+  }
+  SE2_FAIL("source implementation %d: use 0 (pointwise), 2 (cubic-spline kernel) or 3 (P0)", impl);
 }
 
 static int locate_receiver(se2_setup *s, int r)
@@ -549,6 +735,26 @@ int se2_setup_create(const se2_spec *sp, se2_setup **out)
   s->lambda = (double*)xcalloc((size_t)sp->mx * sp->my, sizeof(double));
   s->mu = (double*)xcalloc((size_t)sp->mx * sp->my, sizeof(double));
   s->rho = (double*)xcalloc((size_t)sp->mx * sp->my, sizeof(double));
+  if (!sp->cell_vp && sp->perturb) {
+    /* se2wave.c:1177-1236: three PETSc RAND48 streams (seeds 1, 2, 3), width * drand48() + low */
+    const long ne = (long)sp->mx * sp->my;
+    const double x0[3] = {sp->vp, sp->vs, sp->rho}, dx[3] = {sp->dvp, sp->dvs, sp->drho};
+    double *pv = (double*)xcalloc((size_t)ne, sizeof(double) * 3);
+    int f;
+    for (f = 0; f < 3; f++) {
+      const double lo = x0[f] - dx[f], width = (x0[f] + dx[f]) - lo;
+      uint64_t st = rand48_seeded((long)(f + 1));
+      for (e = 0; e < ne; e++) pv[f * ne + e] = width * rand48_next(&st) + lo;
+    }
+    for (e = 0; e < ne; e++) {
+      const double vp = pv[e], vs = pv[ne + e], rho = pv[2 * ne + e];
+      if (!(rho > 0.0) || !(vs >= 0.0) || !(vp > 0.0)) { free(pv); se2_setup_destroy(s); SE2_FAIL("cell %ld: non-physical material", e); }
+      s->mu[e] = vs * vs * rho;
+      s->lambda[e] = vp * vp * rho - 2.0 * s->mu[e];
+      s->rho[e] = rho;
+    }
+    free(pv);
+  } else
   for (e = 0; e < (long)sp->mx * sp->my; e++) {
     const double vp = sp->cell_vp ? sp->cell_vp[e] : sp->vp;
     const double vs = sp->cell_vs ? sp->cell_vs[e] : sp->vs;
@@ -573,18 +779,103 @@ int se2_setup_create(const se2_spec *sp, se2_setup **out)
     }
 
   /* sources */
-  s->nsrc = sp->nsrc;
-  s->src_elem = (int*)xcalloc((size_t)sp->nsrc, sizeof(int));
-  s->src_gll = (int*)xcalloc((size_t)sp->nsrc, sizeof(int));
-  s->src_vals = (double*)xcalloc((size_t)sp->nsrc * 2 * s->npe, sizeof(double));
-  s->stf_type = (int*)xcalloc((size_t)sp->nsrc, sizeof(int));
-  s->stf_par = (double*)xcalloc((size_t)sp->nsrc * 3, sizeof(double));
-  for (i = 0; i < sp->nsrc; i++) {
-    double dummy;
-    if (locate_source(s, i, &sp->src_xy[2 * i], &sp->src_m[4 * i], sp->nearest_internal_gll)) { se2_setup_destroy(s); return -1; }
-    s->stf_type[i] = sp->stf_type[i];
-    memcpy(&s->stf_par[3 * i], &sp->stf_par[3 * i], 3 * sizeof(double));
-    if (se2_stf_eval(s->stf_type[i], &s->stf_par[3 * i], 1.0e30, &dummy)) { se2_setup_destroy(s); return -1; }
+  s->nsrc_phys = sp->nsrc;
+  if (sp->src_impl < 0) {
+    /* SeismicSourceCreate, SOURCE_IMPL_NEAREST_QPOINT (2995-3243): one entry per source */
+    s->nsrc = sp->nsrc;
+    s->src_elem = (int*)xcalloc((size_t)sp->nsrc, sizeof(int));
+    s->src_gll = (int*)xcalloc((size_t)sp->nsrc, sizeof(int));
+    s->src_owner = (int*)xcalloc((size_t)sp->nsrc, sizeof(int));
+    s->src_vals = (double*)xcalloc((size_t)sp->nsrc * 2 * s->npe, sizeof(double));
+    s->stf_type = (int*)xcalloc((size_t)sp->nsrc, sizeof(int));
+    s->stf_par = (double*)xcalloc((size_t)sp->nsrc * 3, sizeof(double));
+    for (i = 0; i < sp->nsrc; i++) {
+      double dummy;
+      if (locate_source(s, i, &sp->src_xy[2 * i], &sp->src_m[4 * i], sp->nearest_internal_gll)) { se2_setup_destroy(s); return -1; }
+      s->src_owner[i] = (int)i;
+      s->stf_type[i] = sp->stf_type[i];
+      memcpy(&s->stf_par[3 * i], &sp->stf_par[3 * i], 3 * sizeof(double));
+      if (se2_stf_eval(s->stf_type[i], &s->stf_par[3 * i], 1.0e30, &dummy)) { se2_setup_destroy(s); return -1; }
+    }
+  } else {
+    /* assembled source vectors (ElastoDynamicsSourceSetup, 2232-2266) split into per-element
+       entries: every node with a non-zero value belongs to the first element (ascending) that
+       holds it, so the entries add up to the vector exactly; each entry carries its source's STF */
+    const long nn = s->nnodes;
+    double *g = (double*)xcalloc((size_t)nn * 2, sizeof(double));
+    char *taken = (char*)xcalloc((size_t)nn, 1);
+    long cap = 0, ne = 0, e;
+    s->nsrc = 0;
+    for (i = 0; i < sp->nsrc; i++) {
+      double dummy;
+      if (se2_source_vector(s, sp->src_impl, sp->sm_h, &sp->src_xy[2 * i], &sp->src_m[4 * i], g) ||
+          se2_stf_eval(sp->stf_type[i], &sp->stf_par[3 * i], 1.0e30, &dummy)) {
+        free(g); free(taken); se2_setup_destroy(s); return -1;
+      }
+      memset(taken, 0, (size_t)nn);
+      /* candidate elements: those holding a non-zero node */
+      {
+        long *cand = NULL, nc = 0, cc = 0;
+        for (e = 0; e < (long)s->mx * s->my; e++) {
+          const int ei = (int)(e % s->mx), ej = (int)(e / s->mx);
+          int a, b, any = 0;
+          for (b = 0; b < s->n1 && !any; b++)
+            for (a = 0; a < s->n1; a++) {
+              const long node = (long)(ei * s->p + a) + (long)(ej * s->p + b) * s->nx_g;
+              if (g[2 * node] != 0.0 || g[2 * node + 1] != 0.0) { any = 1; break; }
+            }
+          if (!any) continue;
+          if (nc == cc) { cc = cc ? 2 * cc : 16; cand = (long*)realloc(cand, sizeof(long) * (size_t)cc); }
+          cand[nc++] = e;
+        }
+        /* greedy cover: the element with the most unassigned non-zero nodes first (lowest index on ties) */
+        for (;;) {
+          long best = -1, k;
+          int bestn = 0;
+          for (k = 0; k < nc; k++) {
+            const int ei = (int)(cand[k] % s->mx), ej = (int)(cand[k] / s->mx);
+            int a, b, cnt = 0;
+            for (b = 0; b < s->n1; b++)
+              for (a = 0; a < s->n1; a++) {
+                const long node = (long)(ei * s->p + a) + (long)(ej * s->p + b) * s->nx_g;
+                if (!taken[node] && (g[2 * node] != 0.0 || g[2 * node + 1] != 0.0)) cnt++;
+              }
+            if (cnt > bestn) { bestn = cnt; best = cand[k]; }
+          }
+          if (best < 0) break;
+          e = best;
+          {
+            const int ei = (int)(e % s->mx), ej = (int)(e / s->mx);
+            int a, b;
+            if (ne == cap) {
+              cap = cap ? 2 * cap : 16;
+              s->src_elem = (int*)realloc(s->src_elem, sizeof(int) * (size_t)cap);
+              s->src_gll = (int*)realloc(s->src_gll, sizeof(int) * (size_t)cap);
+              s->src_owner = (int*)realloc(s->src_owner, sizeof(int) * (size_t)cap);
+              s->src_vals = (double*)realloc(s->src_vals, sizeof(double) * 2 * (size_t)s->npe * (size_t)cap);
+              s->stf_type = (int*)realloc(s->stf_type, sizeof(int) * (size_t)cap);
+              s->stf_par = (double*)realloc(s->stf_par, sizeof(double) * 3 * (size_t)cap);
+            }
+            s->src_elem[ne] = (int)e;
+            s->src_gll[ne] = -1;
+            s->src_owner[ne] = (int)i;
+            s->stf_type[ne] = sp->stf_type[i];
+            memcpy(&s->stf_par[3 * ne], &sp->stf_par[3 * i], 3 * sizeof(double));
+            for (b = 0; b < s->n1; b++)
+              for (a = 0; a < s->n1; a++) {
+                const long node = (long)(ei * s->p + a) + (long)(ej * s->p + b) * s->nx_g;
+                double *v = &s->src_vals[(size_t)ne * 2 * s->npe + 2 * (a + b * s->n1)];
+                if (!taken[node]) { v[0] = g[2 * node]; v[1] = g[2 * node + 1]; taken[node] = 1; }
+                else { v[0] = 0.0; v[1] = 0.0; }
+              }
+            ne++;
+          }
+        }
+        free(cand);
+      }
+    }
+    s->nsrc = (int)ne;
+    free(g); free(taken);
   }
 
   /* receivers */

@@ -17,6 +17,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <algorithm>
+#include <utility>
 #include <vector>
 
 #include "se2gpu.h"
@@ -702,4 +703,88 @@ extern "C" int se2gpu_set_tile_config(se2gpu_solver *h, int config)
   if (config < 0 || config >= se2p::num_configs(h->p)) return fail(h, SE2GPU_ERR_ARG, "tile configuration %d out of range", config);
   CK(h, cudaSetDevice(h->device));
   return setup_f32_config(h, config);
+}
+
+// ---------------------------------------------------------------- checkpoint / resume
+namespace {
+struct CkptHeader {
+  char magic[8];               // "SE2CKPT1"
+  int precision, mx, my, p, nrec, pitch;
+  int pending_record, rlast;
+  long nnodes;
+};
+
+// the device arrays of the evolving state, in checkpoint order
+std::vector<std::pair<void *, size_t>> state_arrays(se2gpu_solver *h)
+{
+  std::vector<std::pair<void *, size_t>> v;
+  if (is_f64(h)) {
+    const size_t b = (size_t)h->nnodes * 2 * 8;
+    for (int f = 0; f < 3; f++) v.push_back({h->f64[h->cur][f], b});
+  } else {
+    const size_t b = (size_t)h->ny_g * h->pitch * 8;
+    v.push_back({h->pu[h->cur], b});
+    v.push_back({h->pw[h->cur], b});
+    if (is_kahan(h)) { v.push_back({h->pcu[h->cur], b}); v.push_back({h->pcw[h->cur], b}); }
+    v.push_back({h->pa, b});
+    if (h->nrec) v.push_back({h->rbuf[h->rlast], (size_t)h->nrec * h->npe * 6 * 4});
+  }
+  return v;
+}
+}  // namespace
+
+extern "C" long se2gpu_checkpoint_size(const se2gpu_solver *h)
+{
+  if (!h) return SE2GPU_ERR_ARG;
+  long n = (long)sizeof(CkptHeader);
+  for (auto &a : state_arrays(const_cast<se2gpu_solver *>(h))) n += (long)a.second;
+  return n;
+}
+
+extern "C" int se2gpu_checkpoint_save(se2gpu_solver *h, void *buf, long bytes)
+{
+  if (!h || !buf) return SE2GPU_ERR_ARG;
+  if (bytes < se2gpu_checkpoint_size(h)) return fail(h, SE2GPU_ERR_ARG, "checkpoint buffer of %ld bytes, %ld needed", bytes, se2gpu_checkpoint_size(h));
+  if (h->rows_written > 0) return fail(h, SE2GPU_ERR_STATE, "%d trace rows are buffered; fetch them with se2gpu_traces before saving", h->rows_written);
+  CK(h, cudaSetDevice(h->device));
+  CK(h, cudaStreamSynchronize(h->stream));
+  int rc;
+  if ((rc = check_err_flag(h))) return rc;
+  CkptHeader hd;
+  memset(&hd, 0, sizeof(hd));
+  memcpy(hd.magic, "SE2CKPT1", 8);
+  hd.precision = h->precision; hd.mx = h->mx; hd.my = h->my; hd.p = h->p; hd.nrec = h->nrec; hd.pitch = h->pitch;
+  hd.pending_record = h->pending_record ? 1 : 0; hd.rlast = h->rlast; hd.nnodes = h->nnodes;
+  char *o = static_cast<char *>(buf);
+  memcpy(o, &hd, sizeof(hd));
+  o += sizeof(hd);
+  for (auto &a : state_arrays(h)) {
+    CK(h, cudaMemcpy(o, a.first, a.second, cudaMemcpyDeviceToHost));
+    o += a.second;
+  }
+  return 0;
+}
+
+extern "C" int se2gpu_checkpoint_load(se2gpu_solver *h, const void *buf, long bytes)
+{
+  if (!h || !buf) return SE2GPU_ERR_ARG;
+  if (bytes < (long)sizeof(CkptHeader)) return fail(h, SE2GPU_ERR_ARG, "checkpoint too short");
+  CkptHeader hd;
+  memcpy(&hd, buf, sizeof(hd));
+  if (memcmp(hd.magic, "SE2CKPT1", 8) != 0) return fail(h, SE2GPU_ERR_ARG, "not a checkpoint");
+  if (hd.precision != h->precision || hd.mx != h->mx || hd.my != h->my || hd.p != h->p || hd.nrec != h->nrec ||
+      hd.pitch != h->pitch || hd.nnodes != h->nnodes)
+    return fail(h, SE2GPU_ERR_ARG, "checkpoint of another problem or precision (%dx%d p%d precision %d)", hd.mx, hd.my, hd.p, hd.precision);
+  CK(h, cudaSetDevice(h->device));
+  CK(h, cudaStreamSynchronize(h->stream));
+  h->rows_written = 0;
+  h->pending_record = hd.pending_record != 0;
+  if (!is_f64(h)) h->rlast = hd.rlast & 1;
+  if (bytes < se2gpu_checkpoint_size(h)) return fail(h, SE2GPU_ERR_ARG, "checkpoint truncated");
+  const char *o = static_cast<const char *>(buf) + sizeof(hd);
+  for (auto &a : state_arrays(h)) {
+    CK(h, cudaMemcpy(a.first, o, a.second, cudaMemcpyHostToDevice));
+    o += a.second;
+  }
+  return 0;
 }

@@ -139,7 +139,12 @@ static double *read_doubles(const char *fname, long n)
 
 int main(int argc, char **argv)
 {
-  int mx = 8, my, p = 2, nt_opt = -1, of = 5000, block = 100, r, s, ignore_rec, precision;
+  int mx = 8, my, p = 2, nt_opt = -1, of = 5000, block = 100, r, s, ignore_rec, precision, dump_ic, ckpt_every = 0;
+  const char *restart;
+  int sp_src_impl = -1;
+  double sp_sm_h = 0.0;
+  double dvp = 0.0, dvs = 0.0, drho = 0.0;
+  int perturb;
   double tmax = 0.4, dt_opt = 0.0, cfl = 0.5, Lx = 2000.0, Ly, x0 = -1000.0, y0, vp = 4746.3670317412243,
          vs = 2740.2554625435928, rho = 1000.0;
   const char *problem, *prec_s, *rec_file, *cells;
@@ -149,7 +154,7 @@ int main(int argc, char **argv)
   se2gpu_solver *h = NULL;
   double src_xy[8], src_m[16], stf_par[12], *rec_xy = NULL, *cell = NULL;
   int stf_type[4], nsrc, nrec;
-  char fname[512], meta[512];
+  char fname[512], meta[512], fname_vts[512];
   FILE *fp;
   long k, nsteps;
   double time = 0.0;
@@ -161,6 +166,7 @@ int main(int argc, char **argv)
   if (opt_bool("-verify_stf", 0)) return verify_stf();
 
   ignore_rec = opt_bool("-ignore_receiver_output", 0);
+  dump_ic = opt_bool("-dump_ic_src", 0);
   opt_int("-bdegree", &p);
   problem = opt_str("-problem", "demo");
   prec_s = opt_str("-precision", "fp64");
@@ -202,6 +208,8 @@ int main(int argc, char **argv)
   Ly = Lx; y0 = x0;
   opt_real("-Lx", &Lx); opt_real("-Ly", &Ly); opt_real("-x0", &x0); opt_real("-y0", &y0);
   opt_real("-vp", &vp); opt_real("-vs", &vs); opt_real("-rho", &rho); opt_real("-cfl", &cfl);
+  /* -dvp -dvs -drho: per-cell materials from SpecFECtxSetPerturbedMaterialProperties_Velocity */
+  perturb = opt_real("-dvp", &dvp) | opt_real("-dvs", &dvs) | opt_real("-drho", &drho);
   opt_real("-tmax", &tmax);
   rec_file = opt_str("-rec_file", NULL);
   if (rec_file) {
@@ -237,13 +245,35 @@ int main(int argc, char **argv)
   if (opt_real("-dt", &dt_opt)) sp.dt = dt_opt;
   if (opt_int("-nt", &nt_opt)) sp.nt = nt_opt;
   opt_int("-of", &of);
+  if (of < 1) { fprintf(stderr, "-of must be at least 1\n"); return 1; }
   opt_int("-block", &block);
+  opt_int("-checkpoint_every", &ckpt_every);
+  {
+    int impl = -1;
+    double h = 0.0;
+    if (opt_int("-source_impl", &impl)) {  /* ElastoDynamicsSetSourceImplementation (2202-2230) */
+      const char *nm[4] = {"pointwise evaluation", "closest internal basis", "cspline kernel", "P0"};
+      if (impl < 0 || impl > 3) { fprintf(stderr, "-source_impl: valid choices are 0,1,2,3\n"); return 1; }
+      printf("  [source implementation]: processed from command line args\n");
+      printf("  [source implementation]: %s\n", nm[impl]);
+      sp_src_impl = (impl == 1) ? -1 : impl;   /* 1 = the nearest interior GLL point, the default path */
+    }
+    if (opt_real("-sm_h", &h)) sp_sm_h = h;
+  }
+  restart = opt_str("-restart", NULL);
   if (block < 1) block = 1;
   sp.nearest_internal_gll = opt_bool("-use_nearest_internal_gll", 1);
   sp.nsrc = nsrc; sp.src_xy = src_xy; sp.src_m = src_m; sp.stf_type = stf_type; sp.stf_par = stf_par;
   sp.nrec = nrec; sp.rec_xy = rec_xy;
+  if (!cell && perturb) { sp.perturb = 1; sp.dvp = dvp; sp.dvs = dvs; sp.drho = drho; }
+  sp.src_impl = sp_src_impl;
+  sp.sm_h = sp_sm_h;
 
-  if (!cell) {
+  if (!cell && perturb) {  /* se2wave.c:1228-1230 */
+    printf("  [material]     Vp0 = %1.8e : delta = %+1.8e\n", vp, dvp);
+    printf("  [material]     Vs0 = %1.8e : delta = %+1.8e\n", vs, dvs);
+    printf("  [material]    rho0 = %1.8e : delta = %+1.8e\n", rho, drho);
+  } else if (!cell) {
     double mu = vs * vs * rho, lambda = vp * vp * rho - 2.0 * mu;
     printf("  [material]     Vp = %1.8e\n", vp);
     printf("  [material]     Vs = %1.8e\n", vs);
@@ -252,7 +282,7 @@ int main(int argc, char **argv)
     printf("  [material]    rho = %1.8e\n", rho);
   }
   if (se2_setup_create(&sp, &su)) { fprintf(stderr, "[se2wave_gpu] set-up error: %s\n", se2_host_last_error()); return 1; }
-  for (s = 0; s < nsrc; s++) {  /* the demo prints each moment, then SeismicSourceCreate's lines (4626-4652) */
+  for (s = 0; s < nsrc && sp.src_impl < 0; s++) {  /* the demo prints each moment, then SeismicSourceCreate's lines (4626-4652) */
     int g = su->src_gll[s], e = su->src_elem[s], gi = g % su->n1, gj = g / su->n1;
     printf("Moment: [ %+1.2e , %+1.2e ; %+1.2e , %+1.2e ]\n", src_m[4 * s], src_m[4 * s + 1], src_m[4 * s + 2], src_m[4 * s + 3]);
     printf("[SeismicSource] source (%+1.4e,%+1.4e) --> element %d | rank 0\n", src_xy[2 * s], src_xy[2 * s + 1], e);
@@ -263,6 +293,14 @@ int main(int argc, char **argv)
   printf("[se2wave] Requested time period: %1.4e\n", tmax);
   printf("[se2wave] Using time step size: %1.4e\n", su->dt);
   printf("[se2wave] Estimated number of time steps: %ld\n", su->nt);
+
+  if (dump_ic) {  /* initial displacement (zero), se2wave.c:4606-4610 */
+    double *u0 = (double*)calloc((size_t)su->nnodes * 2, sizeof(double));
+    const char *nm[1] = {"disp"};
+    const double *vv[1] = {u0};
+    if (se2_write_vts(su, "uva.vts", 1, nm, vv)) { fprintf(stderr, "%s\n", se2_host_last_error()); return 1; }
+    free(u0);
+  }
 
   memset(&pr, 0, sizeof(pr));
   pr.mx = mx; pr.my = my; pr.p = p; pr.dt = su->dt;
@@ -276,7 +314,7 @@ int main(int argc, char **argv)
   /* receiver files: header of RecordUVA_MultipleStations_NearestGLL_MPI (2808-2882) */
   snprintf(fname, sizeof(fname), "closestqpsource-receiverCP-uva-%dx%d-p%d-rank%d.dat", mx, my, p, 0);
   snprintf(meta, sizeof(meta), "closestqpsource-receiverCP-uva-%dx%d-p%d.mpimeta", mx, my, p);
-  if (!ignore_rec && nrec > 0) {
+  if (!ignore_rec && nrec > 0 && !restart) {
     fp = fopen(fname, "w");
     if (!fp) { fprintf(stderr, "Failed to open file \"%s\"\n", fname); return 1; }
     fprintf(fp, "# SpecFECtx meta data\n");
@@ -311,15 +349,38 @@ int main(int argc, char **argv)
 
   /* the time loop (4722-4775) in device batches that end on the 100-step log lines */
   nsteps = su->nsteps;
+  k = 0;
+  if (restart) {  /* resume: step count, time and the device state of a checkpoint file */
+    FILE *cf = fopen(restart, "rb");
+    char magic[8];
+    long bytes = 0;
+    void *blob;
+    if (!cf || fread(magic, 1, 8, cf) != 8 || memcmp(magic, "SE2RUN01", 8) || fread(&k, sizeof(long), 1, cf) != 1 ||
+        fread(&time, sizeof(double), 1, cf) != 1 || fread(&bytes, sizeof(long), 1, cf) != 1 || bytes <= 0) {
+      fprintf(stderr, "cannot read checkpoint %s\n", restart);
+      return 1;
+    }
+    blob = malloc((size_t)bytes);
+    if (fread(blob, 1, (size_t)bytes, cf) != (size_t)bytes) { fprintf(stderr, "truncated checkpoint %s\n", restart); return 1; }
+    fclose(cf);
+    CHECK(se2gpu_checkpoint_load(h, blob, bytes));
+    free(blob);
+  }
   {
     double *stf = (double*)malloc(sizeof(double) * (size_t)block * (nsrc > 0 ? nsrc : 1));
     double *times = (double*)malloc(sizeof(double) * (size_t)block);
     double *rows = (double*)malloc(sizeof(double) * (size_t)(block + 1) * 7 * (nrec > 0 ? nrec : 1));
     double nrm[6];
-    for (k = 0; k < nsteps;) {
+    double *fu = (double*)malloc(sizeof(double) * 2 * (size_t)su->nnodes);
+    double *fv = (double*)malloc(sizeof(double) * 2 * (size_t)su->nnodes);
+    const char *vnames[2] = {"disp", "velo"};
+    const double *vvecs[2] = {fu, fv};
+    for (; k < nsteps;) {
       long n = block - (k % block);
       long j;
       int nr;
+      if (n > of - (k % of)) n = of - (k % of);   /* end blocks on snapshot steps */
+      if (ckpt_every > 0 && n > ckpt_every - (k % ckpt_every)) n = ckpt_every - (k % ckpt_every);
       if (k + n > nsteps) n = nsteps - k;
       if (se2_stf_block(su, &time, n, times, stf)) { fprintf(stderr, "%s\n", se2_host_last_error()); return 1; }
       CHECK(se2gpu_advance(h, (int)n, stf));
@@ -345,15 +406,39 @@ int main(int argc, char **argv)
         }
         fclose(fp);
       }
+      if (ckpt_every > 0 && k % ckpt_every == 0 && k < nsteps) {  /* checkpoint after the block's rows are out */
+        long bytes = se2gpu_checkpoint_size(h);
+        void *blob = malloc((size_t)bytes);
+        char cname[64];
+        FILE *cf;
+        CHECK(se2gpu_checkpoint_save(h, blob, bytes));
+        snprintf(cname, sizeof(cname), "checkpoint-%06ld.bin", k);
+        cf = fopen(cname, "wb");
+        if (!cf || fwrite("SE2RUN01", 1, 8, cf) != 8 || fwrite(&k, sizeof(long), 1, cf) != 1 ||
+            fwrite(&time, sizeof(double), 1, cf) != 1 || fwrite(&bytes, sizeof(long), 1, cf) != 1 ||
+            fwrite(blob, 1, (size_t)bytes, cf) != (size_t)bytes || fclose(cf) != 0) {
+          fprintf(stderr, "cannot write %s\n", cname);
+          return 1;
+        }
+        free(blob);
+      }
+      if (k % of == 0) {  /* se2wave.c:4764-4770 */
+        snprintf(fname_vts, sizeof(fname_vts), "step-%.4ld.vts", k);
+        CHECK(se2gpu_get_fields(h, fu, fv, NULL));
+        if (se2_write_vts(su, fname_vts, 2, vnames, vvecs)) { fprintf(stderr, "%s\n", se2_host_last_error()); return 1; }
+      }
     }
     /* after the loop the reference prints k: the breaking step, or nt+1 when the loop ran out */
     printf("[step %9ld] time = %1.4e : dt = %1.4e \n", (time >= su->tmax) ? k : k + 1, time, su->dt);
     CHECK(se2gpu_norms(h, nrm));
     printf("  [displacement] max = %+1.4e : min = %+1.4e : l2 = %+1.4e \n", nrm[0], nrm[1], nrm[2]);
     printf("  [velocity]     max = %+1.4e : min = %+1.4e : l2 = %+1.4e \n", nrm[3], nrm[4], nrm[5]);
-    free(stf); free(times); free(rows);
+    /* last snapshot (se2wave.c:4785-4789), named with the same k */
+    snprintf(fname_vts, sizeof(fname_vts), "step-%.4ld.vts", (time >= su->tmax) ? k : k + 1);
+    CHECK(se2gpu_get_fields(h, fu, fv, NULL));
+    if (se2_write_vts(su, fname_vts, 2, vnames, vvecs)) { fprintf(stderr, "%s\n", se2_host_last_error()); return 1; }
+    free(stf); free(times); free(rows); free(fu); free(fv);
   }
-  (void)of;
   se2gpu_destroy(h);
   se2_setup_destroy(su);
   free(rec_xy); free(cell);

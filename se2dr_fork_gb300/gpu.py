@@ -29,7 +29,8 @@ EXPORTS = ["se2gpu_create", "se2gpu_destroy", "se2gpu_last_error", "se2gpu_creat
            "se2gpu_ensemble_set_stream", "se2gpu_ensemble_set_graphs", "se2gpu_ensemble_set_tile_config",
            "se2gpu_ensemble_tile_config", "se2gpu_ensemble_advance", "se2gpu_ensemble_enqueue",
            "se2gpu_ensemble_synchronize", "se2gpu_ensemble_get_fields", "se2gpu_ensemble_set_fields",
-           "se2gpu_ensemble_info", "se2gpu_norms_device_noalloc"]
+           "se2gpu_ensemble_info", "se2gpu_norms_device_noalloc",
+           "se2gpu_checkpoint_size", "se2gpu_checkpoint_save", "se2gpu_checkpoint_load"]
 
 
 class _CProblem(C.Structure):
@@ -89,6 +90,10 @@ def lib():
         L.se2gpu_ensemble_set_fields.argtypes = [vp, C.c_int, _dp, _dp, _dp]
         L.se2gpu_ensemble_info.argtypes = [vp, C.POINTER(C.c_long)]
         L.se2gpu_norms_device_noalloc.argtypes = [vp, vp, C.c_long, vp, _dp]
+        L.se2gpu_checkpoint_size.argtypes = [vp]
+        L.se2gpu_checkpoint_size.restype = C.c_long
+        L.se2gpu_checkpoint_save.argtypes = [vp, vp, C.c_long]
+        L.se2gpu_checkpoint_load.argtypes = [vp, vp, C.c_long]
         _lib = L
     return _lib
 
@@ -248,6 +253,23 @@ class Solver:
     def set_tile_config(self, config: int):
         self._check(lib().se2gpu_set_tile_config(self._h, int(config)), "se2gpu_set_tile_config")
         self.tile_config = int(config)
+
+    def checkpoint(self) -> bytes:
+        """The handle's state (se2gpu_checkpoint_save; buffered trace rows must have been fetched),
+        followed by this binding's time, step count and the times of rows still pending."""
+        n = self._check(lib().se2gpu_checkpoint_size(self._h), "se2gpu_checkpoint_size")
+        buf = C.create_string_buffer(n)
+        self._check(lib().se2gpu_checkpoint_save(self._h, buf, n), "se2gpu_checkpoint_save")
+        pend = np.array(self._times, dtype=np.float64)
+        return buf.raw + pend.tobytes() + np.array([self.time, self.step, len(pend)], dtype=np.float64).tobytes()
+
+    def restore(self, blob: bytes):
+        time_, step, npend = np.frombuffer(blob[-24:], dtype=np.float64)
+        npend = int(npend)
+        body = blob[:len(blob) - 24 - 8 * npend]
+        self._check(lib().se2gpu_checkpoint_load(self._h, body, len(body)), "se2gpu_checkpoint_load")
+        self.time, self.step = float(time_), int(step)
+        self._times = np.frombuffer(blob[len(body):len(blob) - 24], dtype=np.float64).tolist()
 
 
 class Ensemble:

@@ -25,7 +25,9 @@ class _CSpec(C.Structure):
                 ("cfl", C.c_double), ("dt", C.c_double), ("tmax", C.c_double),
                 ("nt", C.c_int), ("nearest_internal_gll", C.c_int),
                 ("nsrc", C.c_int), ("src_xy", _dp), ("src_m", _dp), ("stf_type", _ip), ("stf_par", _dp),
-                ("nrec", C.c_int), ("rec_xy", _dp)]
+                ("nrec", C.c_int), ("rec_xy", _dp),
+                ("perturb", C.c_int), ("dvp", C.c_double), ("dvs", C.c_double), ("drho", C.c_double),
+                ("src_impl", C.c_int), ("sm_h", C.c_double)]
 
 
 class _CSetup(C.Structure):
@@ -39,7 +41,8 @@ class _CSetup(C.Structure):
                 ("nt", C.c_long), ("nsteps", C.c_long),
                 ("nsrc", C.c_int), ("src_elem", _ip), ("src_gll", _ip), ("src_vals", _dp),
                 ("stf_type", _ip), ("stf_par", _dp),
-                ("nrec", C.c_int), ("rec_xy", _dp), ("rec_node", _ip), ("rec_elem", _ip), ("rec_gll", _ip)]
+                ("nrec", C.c_int), ("rec_xy", _dp), ("rec_node", _ip), ("rec_elem", _ip), ("rec_gll", _ip),
+                ("nsrc_phys", C.c_int), ("src_owner", _ip)]
 
 
 class CShotDraw(C.Structure):
@@ -69,6 +72,7 @@ def lib():
         L.se2_stf_eval.argtypes = [C.c_int, _dp, C.c_double, _dp]
         L.se2_gaussian_random_field.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                                 C.c_ulonglong, _dp]
+        L.se2_source_vector.argtypes = [C.POINTER(_CSetup), C.c_int, C.c_double, _dp, _dp, _dp]
         L.se2_shot_draw_params.argtypes = [C.c_ulonglong, C.c_long, C.c_int, C.POINTER(CShotDraw)]
         L.se2_shot_materials.argtypes = [C.POINTER(CShotDraw), _dp, _dp, _dp]
         _lib = L
@@ -107,6 +111,10 @@ class _SpecHolder:
         cs.src_xy, cs.src_m, cs.stf_type, cs.stf_par = _p(sxy), _p(sm), _p(st, _ip), _p(sp)
         cs.nrec = len(spec.receivers)
         cs.rec_xy = _p(rxy)
+        if spec.perturb is not None:
+            cs.perturb = 1
+            cs.dvp, cs.dvs, cs.drho = spec.perturb
+        cs.src_impl, cs.sm_h = int(spec.src_impl), float(spec.sm_h)
         self.cs = cs
 
 
@@ -151,6 +159,8 @@ class Setup:
         self.rec_node = _arr(s.rec_node, self.nrec, np.int32)
         self.rec_elem = _arr(s.rec_elem, self.nrec, np.int32)
         self.rec_gll = _arr(s.rec_gll, self.nrec, np.int32)
+        self.nsrc_phys = s.nsrc_phys
+        self.src_owner = _arr(s.src_owner, self.nsrc, np.int32)
 
     def __del__(self):
         if getattr(self, "_ptr", None):
@@ -169,6 +179,16 @@ class Setup:
     def mass_vec(self) -> np.ndarray:
         """Lumped mass as the reference's interleaved 2-component Vec (Md)."""
         return np.repeat(self.mass, 2)
+
+    def source_vector(self, impl: int, xy, moment, kernel_h: float = 0.0) -> np.ndarray:
+        """Assembled source vector of one moment source (se2_source_vector): impl 0 pointwise,
+        2 cubic-spline kernel (radius kernel_h, <= 0 for the reference's default), 3 P0."""
+        g = np.zeros(self.ndof)
+        xy = np.ascontiguousarray(xy, dtype=np.float64)
+        m = np.ascontiguousarray(moment, dtype=np.float64)
+        if lib().se2_source_vector(self._ptr, int(impl), float(kernel_h), _p(xy), _p(m), _p(g)) != 0:
+            raise ValueError(_err())
+        return g
 
     def stf_block(self, time: float, n: int) -> Tuple[np.ndarray, np.ndarray, float]:
         """Times and STF values of the next n steps after `time`."""

@@ -65,6 +65,13 @@ class Spec:
     sources: List[Source] = field(default_factory=list)
     receivers: List[Tuple[float, float]] = field(default_factory=list)
     name: str = "custom"
+    # (dvp, dvs, drho): cell materials uniform in [vp - dvp, vp + dvp] etc. from PETSc's RAND48
+    # (SpecFECtxSetPerturbedMaterialProperties_Velocity, se2wave.c:1177-1236)
+    perturb: Optional[Tuple[float, float, float]] = None
+    # source representation: -1 SeismicSourceCreate's nearest GLL point (the demo's); 0 pointwise,
+    # 2 cubic-spline kernel of radius sm_h (<= 0: default), 3 P0 (se2wave.c:2202-2266, -source_impl)
+    src_impl: int = -1
+    sm_h: float = 0.0
 
     @property
     def ne(self) -> int:
@@ -107,6 +114,8 @@ class Spec:
                  f"cfl {self.cfl!r}", f"dt {self.dt!r}", f"tmax {self.tmax!r}", f"nt {self.nt}"]
         if cell_file:
             lines.append(f"cell_file {cell_file}")
+        if self.perturb is not None:
+            lines.append("perturb " + " ".join(repr(float(v)) for v in self.perturb))
         for s in self.sources:
             m = " ".join(repr(float(v)) for v in s.moment)
             par = " ".join(repr(float(v)) for v in s.par)

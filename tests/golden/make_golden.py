@@ -67,7 +67,29 @@ def spec_arrays(sp: S.Spec) -> dict:
              rec_xy=np.array(sp.receivers, dtype=np.float64).reshape(-1, 2))
     if sp.cell_vp is not None:
         d.update(cell_vp=np.asarray(sp.cell_vp), cell_vs=np.asarray(sp.cell_vs), cell_rho=np.asarray(sp.cell_rho))
+    if sp.perturb is not None:
+        d.update(perturb=np.array(sp.perturb, dtype=np.float64))
     return {"spec_" + k: v for k, v in d.items()}
+
+
+def source_vectors():
+    """Assembled source vectors of the alternative source representations (se2wave.c:1716-2200)."""
+    for p in (2, 4, 6):
+        sp = S.demo(9, 7, p=p, tmax=1.0).replace(nt=5, name=f"srcvec_p{p}",
+                                                  sources=[S.Source(137.3, -251.9, (1e15, 3e14, -2e14, 5e14))])
+        out = {f"g_impl{i}": O.ref_source_vector(sp, i) for i in (0, 2, 3)}
+        out["g_impl2_h310p5"] = O.ref_source_vector(sp, 2, ["-sm_h", "310.5"])
+        save(f"srcvec_p{p}", **out, **spec_arrays(sp))
+
+
+def perturbed():
+    """SpecFECtxSetPerturbedMaterialProperties_Velocity (se2wave.c:1177-1236) on the demo."""
+    sp = S.demo(9, 7, p=3, tmax=1.0).replace(nt=60, perturb=(500.0, 200.0, 100.0), name="perturbed_p3")
+    r = O.ref_run(sp)
+    if r["returncode"] != 0:
+        raise RuntimeError(r["stderr"])
+    res = run_case(sp, fields=True)
+    save("perturbed_p3", cell_lmr=r["cell_lmr"], **res, **spec_arrays(sp))
 
 
 def run_case(sp: S.Spec, fields: bool, extra=()):
@@ -103,6 +125,11 @@ def reference_main_outputs(args, name):
 
 
 def main():
+    if "--perturbed-only" in sys.argv:
+        O.build_ref()
+        perturbed()
+        source_vectors()
+        return
     if "--cli-only" in sys.argv:
         O.build_ref()
         reference_main_outputs([], "cli_demo_default")
@@ -121,6 +148,9 @@ def main():
     save("ragged_p4", **run_case(sp, fields=True), **spec_arrays(sp))
     sp = S.demo(8, p=2)
     save("demo8_p2", **run_case(sp, fields=True), **spec_arrays(sp))
+
+    perturbed()
+    source_vectors()
 
     print("internal force AssembleLinearForm_ElastoDynamics2d on random displacements")
     for p, mx, my in [(1, 6, 5), (3, 6, 5), (4, 9, 10), (7, 3, 4)]:

@@ -24,6 +24,8 @@ def spec_of(d) -> S.Spec:
                 sources=srcs, receivers=[tuple(r) for r in g("rec_xy")])
     if "spec_cell_vp" in d:
         sp = sp.replace(cell_vp=g("cell_vp"), cell_vs=g("cell_vs"), cell_rho=g("cell_rho"))
+    if "spec_perturb" in d:
+        sp = sp.replace(perturb=tuple(float(x) for x in g("perturb")))
     return sp
 
 

@@ -63,3 +63,78 @@ def test_app_verify_stf_matches_reference_ricker(tmp_path):
     from oracle import oracle as O
     ref = O.stf(0, (0.15, 12.0, 1.0), 0.0, 1.0e-4, 101)  # the literals the reference uses (se2wave.c:4837)
     np.testing.assert_allclose(vals, ref, rtol=1e-11, atol=1e-300)
+
+
+def read_vts(path):
+    """Arrays of a VTK XML StructuredGrid file with raw appended data (UInt64 headers)."""
+    import re
+    blob = open(path, "rb").read()
+    head, _, tail = blob.partition(b"<AppendedData encoding=\"raw\">")
+    data = tail[tail.index(b"_") + 1:]
+    ext = [int(v) for v in re.search(rb'WholeExtent="([^"]+)"', head).group(1).split()]
+    out = {}
+    for m in re.finditer(rb'<DataArray type="Float64" Name="([^"]+)" NumberOfComponents="(\d)" format="appended" '
+                         rb'offset="(\d+)"', head):
+        name, nc, off = m.group(1).decode(), int(m.group(2)), int(m.group(3))
+        nbytes = int(np.frombuffer(data[off:off + 8], dtype=np.uint64)[0])
+        out[name] = np.frombuffer(data[off + 8:off + 8 + nbytes], dtype=np.float64).reshape(-1, nc)
+    return (ext[1] + 1, ext[3] + 1), out
+
+
+@pytest.mark.gpu
+def test_app_vts_snapshots_match_oracle_fields(app, tmp_path):
+    """-dump_ic_src and -of write the initial displacement and periodic (u, v)
+    snapshots named as the reference names them; the fields equal the oracle's
+    (FP64, bit for bit) at those steps, and the last snapshot carries the loop's k."""
+    from oracle import oracle as O
+    from se2dr_fork_gb300 import host as H
+    from se2dr_fork_gb300 import spec as S
+    r = subprocess.run([app, "-mx", "6", "-my", "4", "-bdegree", "3", "-tmax", "0.5", "-of", "20", "-dump_ic_src"],
+                       cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    sp = S.demo(6, 4, p=3, tmax=0.5)
+    su = H.Setup(sp)
+    (nx, ny), ic = read_vts(tmp_path / "uva.vts")
+    assert (nx, ny) == (su.nx_g, su.ny_g) and set(ic) == {"Position", "disp_x", "disp_y"}
+    assert np.array_equal(ic["Position"][:, 0], np.tile(su.xnode, ny)) and np.all(ic["disp_x"] == 0)
+    ref = O.OracleSolver(sp)
+    done = 0
+    snaps = sorted(f for f in os.listdir(tmp_path) if f.startswith("step-"))
+    steps = [int(f[5:-4]) for f in snaps]
+    assert steps[:2] == [20, 40] and all(s % 20 == 0 for s in steps[:-1])
+    t = 0.0
+    for _ in range(su.nsteps):
+        t += su.dt                      # time as the loop accumulates it (se2wave.c:4724)
+    last = su.nsteps if t >= su.tmax else su.nsteps + 1
+    assert steps[-1] == last
+    for f, k in zip(snaps, steps):
+        done += ref.run(min(k, su.nsteps) - done, traces=False)["nsteps"]
+        u, v, _ = ref.state()
+        _, arrs = read_vts(tmp_path / f)
+        assert np.array_equal(arrs["disp_x"][:, 0], u[0::2]) and np.array_equal(arrs["disp_y"][:, 0], u[1::2]), f
+        assert np.array_equal(arrs["velo_x"][:, 0], v[0::2]) and np.array_equal(arrs["velo_y"][:, 0], v[1::2]), f
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "fp32_kahan"])
+def test_app_checkpoint_restart_continues_bitwise(app, tmp_path, precision):
+    """-checkpoint_every writes resumable states; -restart from one reproduces the rest of the
+    uninterrupted run: the same receiver rows, snapshots and final log lines."""
+    args = ["-mx", "6", "-my", "4", "-bdegree", "3", "-tmax", "2.0", "-of", "60", "-precision", precision]
+    a, b = tmp_path / "a", tmp_path / "b"
+    a.mkdir()
+    b.mkdir()
+    ra = subprocess.run([app, *args, "-checkpoint_every", "50"], cwd=a, capture_output=True, text=True, timeout=300)
+    assert ra.returncode == 0, ra.stderr
+    assert "checkpoint-000050.bin" in os.listdir(a)
+    rb = subprocess.run([app, *args, "-restart", str(a / "checkpoint-000100.bin")], cwd=b, capture_output=True,
+                        text=True, timeout=300)
+    assert rb.returncode == 0, rb.stderr
+    dat = [f for f in os.listdir(a) if f.endswith(".dat")][0]
+    rows_a = [l for l in open(a / dat) if not l.startswith("#")]
+    rows_b = open(b / dat).read().splitlines(keepends=True)
+    assert len(rows_b) == len(rows_a) - 100 and rows_b == rows_a[100:]
+    assert ra.stdout.splitlines()[-3:] == rb.stdout.splitlines()[-3:]
+    for f in os.listdir(b):
+        if f.endswith(".vts"):
+            assert open(a / f, "rb").read() == open(b / f, "rb").read(), f

@@ -55,6 +55,16 @@ def test_fp64_internal_force_bitwise_vs_reference(p):
     assert np.array_equal(F, d["force"])
 
 
+def test_fp64_perturbed_materials_bitwise_vs_reference():
+    """Cell materials from SpecFECtxSetPerturbedMaterialProperties_Velocity (RAND48), traces and
+    final fields against the reference run on them."""
+    d = load("perturbed_p3")
+    sol = G.Solver(H.Setup(spec_of(d)), "fp64")
+    assert np.array_equal(sol.run(), d["traces"])
+    u, v, a = sol.fields()
+    assert np.array_equal(u, d["u"]) and np.array_equal(v, d["v"]) and np.array_equal(a, d["a"])
+
+
 def test_fp64_explosion64_full_run_bitwise_vs_reference():
     d = load("explosion64")
     sol = G.Solver(H.Setup(spec_of(d)), "fp64")
@@ -248,3 +258,55 @@ def test_fp32_tile_configs_agree(p, precision):
             ref = out
         else:
             assert all(np.array_equal(x, y) for x, y in zip(out, ref)), c
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32_kahan", "fp32"])
+def test_checkpoint_resume_is_bitwise(precision):
+    """Stop after 37 steps, checkpoint, resume in a new handle: identical traces and fields."""
+    d = load("hetero_p4")
+    setup = H.Setup(spec_of(d))
+    ref = G.Solver(setup, precision)
+    tr_ref = np.concatenate([ref.run(37), ref.run(23)])
+    a = G.Solver(setup, precision)
+    tr_a = a.run(37)
+    blob = a.checkpoint()
+    a.close()
+    b = G.Solver(setup, precision)
+    b.restore(blob)
+    tr_b = b.run(23)
+    assert np.array_equal(np.concatenate([tr_a, tr_b]), tr_ref)
+    assert all(np.array_equal(x, y) for x, y in zip(b.fields(), ref.fields()))
+
+
+def test_checkpoint_rejects_other_problems_and_buffered_rows():
+    d = load("hetero_p4")
+    s1 = H.Setup(spec_of(d))
+    a = G.Solver(s1, "fp64")
+    a.advance(3)
+    with pytest.raises(G.GpuError, match="buffered"):
+        a.checkpoint()
+    a.traces()
+    blob = a.checkpoint()
+    other = G.Solver(H.Setup(spec_of(load("hetero_p3"))), "fp64")
+    with pytest.raises(G.GpuError, match="another problem"):
+        other.restore(blob)
+    with pytest.raises(G.GpuError, match="another problem"):
+        G.Solver(s1, "fp32").restore(blob)
+
+
+@pytest.mark.parametrize("impl", [0, 2, 3])
+def test_alternative_source_representations_run(impl):
+    """Source vectors of the pointwise, cubic-spline and P0 representations (their set-up is pinned
+    bitwise against the reference on the host) drive the device loop: exactly linear in the moment in
+    FP64, and FP32-Kahan within its error bars."""
+    sp = spec_of(load("srcvec_p4")).replace(src_impl=impl, nt=120, receivers=[(300.0, 400.0), (-700.0, 150.0)],
+                                            sources=[S.Source(137.3, -251.9, (1e15, 3e14, -2e14, 5e14),
+                                                              S.STF_RICKER, (0.05, 8.0, 1.0))])
+    t1 = G.Solver(H.Setup(sp), "fp64").run()
+    sp2 = sp.replace(sources=[S.Source(137.3, -251.9, (2e15, 6e14, -4e14, 1e15), S.STF_RICKER, (0.05, 8.0, 1.0))])
+    t2 = G.Solver(H.Setup(sp2), "fp64").run()
+    assert np.abs(t1[:, 1:]).max() > 0
+    assert np.array_equal(t2[:, 1:], 2.0 * t1[:, 1:])
+    t32 = G.Solver(H.Setup(sp), "fp32_kahan").run()
+    ok, errs = fp32_errors_ok(t32, t1, k=2 * np.pi * 8.0 / sp.vs)
+    assert ok, errs

@@ -119,3 +119,52 @@ def test_nsteps_matches_reference_loop():
     d = load("explosion64")
     s = H.Setup(spec_of(d))
     assert s.nsteps == 4524 == d["traces"].shape[0]
+
+
+def test_perturbed_materials_bitwise_vs_reference():
+    """SpecFECtxSetPerturbedMaterialProperties_Velocity (RAND48 seeds 1, 2, 3), run by the reference."""
+    from golden_util import load, spec_of
+    from oracle import oracle as O
+    d = load("perturbed_p3")
+    sp = spec_of(d)
+    su = H.Setup(sp)
+    lmr = d["cell_lmr"].reshape(3, -1)
+    assert np.array_equal(su.lam, lmr[0]) and np.array_equal(su.mu, lmr[1]) and np.array_equal(su.rho, lmr[2])
+    assert np.array_equal(O.OracleSolver(sp).get("cell_lmr").reshape(3, -1), lmr)
+    assert len(np.unique(su.rho)) == su.mx * su.my
+    assert np.all(np.abs(su.rho - sp.rho) <= sp.perturb[2])
+
+
+@pytest.mark.parametrize("p", [2, 4, 6])
+def test_alternative_source_vectors_bitwise_vs_reference(p):
+    """Pointwise (1716-1923), cubic-spline kernel (1925-2057, default radius and -sm_h) and P0
+    (2059-2200) source vectors, against the reference's own assembly routines."""
+    d = load(f"srcvec_p{p}")
+    sp = spec_of(d)
+    su = H.Setup(sp)
+    src = sp.sources[0]
+    for impl, h, key in [(0, 0.0, "g_impl0"), (2, 0.0, "g_impl2"), (3, 0.0, "g_impl3"), (2, 310.5, "g_impl2_h310p5")]:
+        g = su.source_vector(impl, (src.x, src.y), src.moment, h)
+        assert np.array_equal(g, d[key]), key
+
+
+@pytest.mark.parametrize("impl", [0, 2, 3])
+def test_source_entries_reassemble_the_vector(impl):
+    d = load("srcvec_p4")
+    sp = spec_of(d)
+    base = H.Setup(sp)
+    g = base.source_vector(impl, (sp.sources[0].x, sp.sources[0].y), sp.sources[0].moment)
+    su = H.Setup(sp.replace(src_impl=impl))
+    assert su.nsrc_phys == 1 and np.all(su.src_owner == 0)
+    assert (su.nsrc == 1) == (impl != 2)
+    acc = np.zeros_like(g)
+    n1 = su.n1
+    for k in range(su.nsrc):
+        e = su.src_elem[k]
+        ex, ey = e % su.mx, e // su.mx
+        for q in range(su.npe):
+            node = (ex * su.p + q % n1) + (ey * su.p + q // n1) * su.nx_g
+            acc[2 * node:2 * node + 2] += su.src_vals[k, 2 * q:2 * q + 2]
+    assert np.array_equal(acc, g)
+    times, stf, _ = su.stf_block(0.0, 7)
+    assert stf.shape == (7, su.nsrc) and np.all(stf == stf[:, :1])
