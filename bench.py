@@ -487,6 +487,52 @@ def run_surrogate(args):
     print(json.dumps(line), flush=True)
 
 
+def run_nn_step(args):
+    """The surrogate network's training step alone (forward, backward, Adam) on resident random
+    inputs: device-timed samples/s and tensor-core TFLOP/s against the measured bf16 peak."""
+    import torch
+    from se2dr_fork_gb300 import nn as N
+    from se2dr_fork_gb300 import surrogate as SU
+    torch.cuda.set_device(0)
+    cfg = SU.net_config(args.nn_batch)
+    net = N.Network(cfg, seed=0)
+    stream = torch.cuda.Stream()
+    net.set_stream(stream.cuda_stream)
+    g = torch.Generator(device="cuda").manual_seed(0)
+    with torch.cuda.stream(stream):
+        x = torch.zeros(args.nn_batch, cfg.ny, cfg.nx, cfg.cin, device="cuda", dtype=torch.bfloat16)
+        x[..., :6] = torch.randn(args.nn_batch, cfg.ny, cfg.nx, 6, device="cuda", generator=g).to(torch.bfloat16)
+        t = torch.randn(args.nn_batch, cfg.nrec, cfg.nout, device="cuda", generator=g)
+    for _ in range(args.warmup):
+        net.loss_grad(x, t)
+        net.adam_step(1e-4)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        net.loss_grad(x, t)
+        net.adam_step(1e-4)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    secs = ev0.elapsed_time(ev1) / 1e3
+    fwd = SU.forward_flops(cfg)
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f)["bf16_tflops"])
+        kind = "measured"
+    except Exception:
+        peak, kind = 1900.0, "fallback"
+    sps = args.steps * args.nn_batch / secs
+    tf = 3 * fwd * sps / 1e12
+    print(json.dumps({"metric": "surrogate training samples/s", "value": sps, "unit": "samples/s", "n_gpus": 1,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+                      "higher_is_better": True, "dtype": "bf16", "data": "synthetic",
+                      "config": {"workload": "training step of the 4-layer, width-64, 16-mode operator on 128^2 "
+                                             f"cells, batch {args.nn_batch}", "flops_per_sample": 3 * fwd},
+                      "roofline": {"bound": "tensor", "achieved": tf, "peak": peak, "unit": "TFLOP/s",
+                                   "frac": tf / peak, "peak_kind": kind, "traffic": None}}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -512,6 +558,8 @@ def main():
     ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--threshold", type=float, default=0.01)
+    ap.add_argument("--nn-step", action="store_true", help="time the surrogate's training step alone")
+    ap.add_argument("--nn-batch", type=int, default=32)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -523,6 +571,8 @@ def main():
         run_ensemble(args)
     elif args.surrogate and args.impl == "ours":
         run_surrogate(args)
+    elif args.nn_step and args.impl == "ours":
+        run_nn_step(args)
     elif args.impl == "reference":
         run_reference(args, rank, world)
     else:

@@ -166,28 +166,56 @@ __global__ void __launch_bounds__(GTHREADS) gemm_bf16(const GemmArgs g)
     __syncthreads();
   }
 
-  // epilogue: accumulator element r of tile (i, j) is (row gid + 8*(r/2), column 2*tig + r%2)
+  // epilogue: accumulator element r of tile (i, j) is (row gid + 8*(r/2), column 2*tig + r%2);
+  // the two columns of a row are handled as a pair (one 4- or 8-byte access) when aligned
+  const bool c_pair = (((g.ldc | g.sC) & 1) == 0) && ((reinterpret_cast<uintptr_t>(g.C) & (g.c_f32 ? 7 : 3)) == 0);
+  const bool in_pair = g.Cin && (((g.ldcin | g.sCin) & 1) == 0) &&
+                       ((reinterpret_cast<uintptr_t>(g.Cin) & (g.cin_f32 ? 7 : 3)) == 0);
+  const bool aux_pair = g.aux && (((g.ldaux | g.sAux) & 1) == 0) && ((reinterpret_cast<uintptr_t>(g.aux) & 3) == 0);
 #pragma unroll
   for (int i = 0; i < 2; i++)
 #pragma unroll
     for (int j = 0; j < 4; j++)
 #pragma unroll
-      for (int r = 0; r < 4; r++) {
-        const int m = m0 + wm + i * 16 + gid + 8 * (r >> 1);
-        const int n = n0 + wn + j * 8 + tig * 2 + (r & 1);
+      for (int hf = 0; hf < 2; hf++) {
+        const int m = m0 + wm + i * 16 + gid + 8 * hf;
+        const int n = n0 + wn + j * 8 + tig * 2;
         if (m >= g.M || n >= g.N) continue;
-        float v = g.alpha * acc[i][j][r];
+        const bool two = (n + 1 < g.N);
+        float v[2] = {g.alpha * acc[i][j][2 * hf], g.alpha * acc[i][j][2 * hf + 1]};
         if (g.Cin && g.beta != 0.f) {
           const long o = (long)b * g.sCin + (long)m * g.ldcin + n;
-          v += g.beta * (g.cin_f32 ? static_cast<const float *>(g.Cin)[o]
-                                   : __bfloat162float(static_cast<const bf16 *>(g.Cin)[o]));
+          if (two && in_pair) {
+            if (g.cin_f32) {
+              const float2 c = *reinterpret_cast<const float2 *>(static_cast<const float *>(g.Cin) + o);
+              v[0] += g.beta * c.x; v[1] += g.beta * c.y;
+            } else {
+              const __nv_bfloat162 c = *reinterpret_cast<const __nv_bfloat162 *>(static_cast<const bf16 *>(g.Cin) + o);
+              v[0] += g.beta * __low2float(c); v[1] += g.beta * __high2float(c);
+            }
+          } else {
+            for (int t = 0; t < (two ? 2 : 1); t++)
+              v[t] += g.beta * (g.cin_f32 ? static_cast<const float *>(g.Cin)[o + t]
+                                          : __bfloat162float(static_cast<const bf16 *>(g.Cin)[o + t]));
+          }
         }
-        if (g.bias) v += g.bias[n];
-        if (g.aux) g.aux[(long)b * g.sAux + (long)m * g.ldaux + n] = __float2bfloat16(v);
-        if (g.act == 1) v = gelu_f(v);
+        if (g.bias) { v[0] += g.bias[n]; if (two) v[1] += g.bias[n + 1]; }
+        if (g.aux) {
+          const long o = (long)b * g.sAux + (long)m * g.ldaux + n;
+          if (two && aux_pair) *reinterpret_cast<__nv_bfloat162 *>(g.aux + o) = __floats2bfloat162_rn(v[0], v[1]);
+          else for (int t = 0; t < (two ? 2 : 1); t++) g.aux[o + t] = __float2bfloat16(v[t]);
+        }
+        if (g.act == 1) { v[0] = gelu_f(v[0]); v[1] = gelu_f(v[1]); }
         const long o = (long)b * g.sC + (long)m * g.ldc + n;
-        if (g.c_f32) static_cast<float *>(g.C)[o] = v;
-        else static_cast<bf16 *>(g.C)[o] = __float2bfloat16(v);
+        if (two && c_pair) {
+          if (g.c_f32) *reinterpret_cast<float2 *>(static_cast<float *>(g.C) + o) = make_float2(v[0], v[1]);
+          else *reinterpret_cast<__nv_bfloat162 *>(static_cast<bf16 *>(g.C) + o) = __floats2bfloat162_rn(v[0], v[1]);
+        } else {
+          for (int t = 0; t < (two ? 2 : 1); t++) {
+            if (g.c_f32) static_cast<float *>(g.C)[o + t] = v[t];
+            else static_cast<bf16 *>(g.C)[o + t] = __float2bfloat16(v[t]);
+          }
+        }
       }
 }
 
