@@ -36,7 +36,7 @@ struct Group {
   std::vector<int> shots;                  // ensemble shot indices, ascending
   se2p::Params *tab[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};   // [input buffer][slot], device
   CUtensorMap *maps[2] = {nullptr, nullptr};                           // [input buffer], device [shot][4]
-  int2 *items = nullptr;                                               // device (local shot, tile)
+  int2 *items = nullptr;                                               // device (local shot, ty << 16 | tx)
 };
 
 }  // namespace
@@ -169,7 +169,8 @@ static int build_group(se2gpu_ensemble *e, Group &g)
   }
   for (int i = 0; i < ns; i++) {
     se2gpu_solver *h = e->sol[g.shots[i]];
-    for (int t = 0; t < h->pntx * h->pnty; t++) items.push_back(make_int2(i, t));
+    if (h->pntx >= 32768 || h->pnty >= 32768) return efail(e, SE2GPU_ERR_ARG, "shot %d: more than 32767 tiles along an axis", g.shots[i]);
+    for (int t = 0; t < h->pntx * h->pnty; t++) items.push_back(make_int2(i, ((t / h->pntx) << 16) | (t % h->pntx)));
   }
   g.nitems = (int)items.size();
   int rc = dput(e, &g.items, items.data(), items.size());

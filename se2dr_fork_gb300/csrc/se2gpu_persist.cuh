@@ -139,10 +139,9 @@ struct TileBox {
 };
 
 template <int P, int TE>
-__device__ __forceinline__ TileBox tile_box(const Params &prm, int t)
+__device__ __forceinline__ TileBox tile_box(const Params &prm, int tx, int ty)
 {
   TileBox b;
-  const int tx = t % prm.ntx, ty = t / prm.ntx;
   b.ex0 = tx * TE; b.ex1 = min(b.ex0 + TE, prm.mx);
   b.ey0 = ty * TE; b.ey1 = min(b.ey0 + TE, prm.my);
   b.EX0 = max(b.ex0 - 1, 0); b.EY0 = max(b.ey0 - 1, 0);
@@ -158,12 +157,12 @@ __device__ __forceinline__ TileBox tile_box(const Params &prm, int t)
 
 // issue the copies of tile t into a stage
 template <int P, int TE, bool KAHAN>
-__device__ __forceinline__ void issue_tile(const Params &prm, int t, unsigned char *stage, uint32_t bar,
+__device__ __forceinline__ void issue_tile(const Params &prm, int tx, int ty, unsigned char *stage, uint32_t bar,
                                            const CUtensorMap *tm_u, const CUtensorMap *tm_cu,
                                            const CUtensorMap *tm_w, const CUtensorMap *tm_cw)
 {
   typedef Layout<P, TE, KAHAN> L;
-  const TileBox b = tile_box<P, TE>(prm, t);
+  const TileBox b = tile_box<P, TE>(prm, tx, ty);
   mbar_expect_tx(bar, L::TX_BYTES);
   size_t o = 0;
   tma_load_2d(smem_u32(stage + o), tm_u, b.RXa, b.RYa, bar); o += L::REG;
@@ -204,7 +203,7 @@ __device__ void sample_rows(const Params &prm, const float *rbuf_in, double *tra
 // one tile: prefetch of global values, wait for the tile's copies, the three
 // element phases and the node phase.  Returns false when the bounded wait expired.
 template <int P, int TE, int NT, bool KAHAN>
-__device__ __forceinline__ bool tile_body(const Params &prm, int t, const unsigned char *st, uint32_t bar,
+__device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, const unsigned char *st, uint32_t bar,
                                           uint32_t parity, float2 *X1, float2 *X2, int item, int el, int j, int ecx,
                                           int ecy, const float (&Dcj)[P + 1], float wj)
 {
@@ -213,7 +212,8 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int t, const unsign
   constexpr int N1 = G::N1, NPE = G::NPE, NEX = G::NEX, BXW = G::BXW, OBW = G::OBW;
   const float *D = c_D[P - 1];
   const float *W = c_w[P - 1];
-  const TileBox b = tile_box<P, TE>(prm, t);
+  const TileBox b = tile_box<P, TE>(prm, tx, ty);
+  const int t = ty * prm.ntx + tx;
   const int xoff = b.EX0 * P - b.RXa;   // region-box column of the first region node
   const bool active = (item < G::ITEMS) && (ecx < b.NEXa) && (ecy < b.NEYa);
   const int ex = b.EX0 + ecx, ey = b.EY0 + ecy;
@@ -351,16 +351,17 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int t, const unsign
     for (int h = 0; h < 2; h++) {
       if (!(h ? v1 : v0)) continue;
       const int X = XA + h;
-      const int exB = X / P, eyB = Y / P;
-      const int exA = (X - exB * P == 0) ? exB - 1 : exB, eyA = (Y - eyB * P == 0) ? eyB - 1 : eyB;
-      for (int e_y = eyA; e_y <= eyB; e_y++) {
-        if (e_y < 0 || e_y >= prm.my) continue;
-        for (int e_x = exA; e_x <= exB; e_x++) {
-          if (e_x < 0 || e_x >= prm.mx) continue;
-          const float2 fe = X1[((e_y - b.EY0) * NEX + (e_x - b.EX0)) * NPE + (X - e_x * P) + (Y - e_y * P) * N1];
-          f[h][0] += fe.x; f[h][1] += fe.y;
-        }
-      }
+      // the 1, 2 or 4 elements around the node, in ascending element order (diagonal,
+      // below, left, own), addressed relative to the node's own element in the region
+      const int lx = X - b.EX0 * P, ly = Y - b.EY0 * P;
+      const int ex = lx / P, ey = ly / P, ix = lx - ex * P, iy = ly - ey * P;
+      const bool in_x = X < prm.mx * P, in_y = Y < prm.my * P;
+      const bool lft = (ix == 0) && (X > 0), bot = (iy == 0) && (Y > 0);
+      const int own = (ey * NEX + ex) * NPE + ix + iy * N1;
+      if (bot && lft) { const float2 fe = X1[own - NEX * NPE - NPE + P + P * N1]; f[h][0] += fe.x; f[h][1] += fe.y; }
+      if (bot && in_x) { const float2 fe = X1[own - NEX * NPE + P * N1]; f[h][0] += fe.x; f[h][1] += fe.y; }
+      if (lft && in_y) { const float2 fe = X1[own - NPE + P]; f[h][0] += fe.x; f[h][1] += fe.y; }
+      if (in_x && in_y) { const float2 fe = X1[own]; f[h][0] += fe.x; f[h][1] += fe.y; }
       for (int q = s0; q < s1; q++) {
         const int sidx = prm.tile_src_idx[q], se = prm.src_elem[sidx], sx = se % prm.mx, sy = se / prm.mx;
         const int a = X - sx * P, bb = Y - sy * P;
@@ -468,19 +469,24 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
   for (int k = 0; k < N1; k++) Dcj[k] = (item < G::ITEMS) ? D[k * N1 + j] : 0.f;
   const float wj = (item < G::ITEMS) ? W[j] : 0.f;
 
+  // tile coordinates advance by the grid size without a division per tile
   int t = blockIdx.x;
-  if (t < prm.ntiles && threadIdx.x == 0) issue_tile<P, TE, KAHAN>(prm, t, stage0, bar0, &tm_u, &tm_cu, &tm_w, &tm_cw);
+  int tx = t % prm.ntx, ty = t / prm.ntx;
+  const int dtx = gridDim.x % prm.ntx, dty = gridDim.x / prm.ntx;
+  if (t < prm.ntiles && threadIdx.x == 0) issue_tile<P, TE, KAHAN>(prm, tx, ty, stage0, bar0, &tm_u, &tm_cu, &tm_w, &tm_cw);
   for (int it = 0; t < prm.ntiles; it++, t += gridDim.x) {
     const int s = it & 1;
     const uint32_t bar = s ? bar1 : bar0;
     const uint32_t parity = (it >> 1) & 1;
+    int txn = tx + dtx, tyn = ty + dty;
+    if (txn >= prm.ntx) { txn -= prm.ntx; tyn++; }
     // prefetch the next tile into the other stage (freed by the barrier that ended the previous tile)
     const int tn = t + gridDim.x;
     if (threadIdx.x == 0 && tn < prm.ntiles) {
       fence_proxy_async();
-      issue_tile<P, TE, KAHAN>(prm, tn, s ? stage0 : stage1, s ? bar0 : bar1, &tm_u, &tm_cu, &tm_w, &tm_cw);
+      issue_tile<P, TE, KAHAN>(prm, txn, tyn, s ? stage0 : stage1, s ? bar0 : bar1, &tm_u, &tm_cu, &tm_w, &tm_cw);
     }
-    if (!tile_body<P, TE, NT, KAHAN>(prm, t, s ? stage1 : stage0, bar, parity, X1, X2, item, el, j, ecx, ecy, Dcj, wj)) {
+    if (!tile_body<P, TE, NT, KAHAN>(prm, tx, ty, s ? stage1 : stage0, bar, parity, X1, X2, item, el, j, ecx, ecy, Dcj, wj)) {
       if (threadIdx.x == 0) {
         atomicExch(prm.err, 1);
         // let this CTA's copies in flight land before the shared memory is released
@@ -489,6 +495,8 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
       }
       return;
     }
+    tx = txn;
+    ty = tyn;
   }
 }
 
@@ -550,7 +558,7 @@ persist_batch(const BatchArgs ba)
   if (w < ba.nitems && threadIdx.x == 0) {
     const int2 wt = ba.items[w];
     const CUtensorMap *m = ba.maps + 4 * wt.x;
-    issue_tile<P, TE, KAHAN>(ba.shots[wt.x], wt.y, stage0, bar0, m, m + 1, m + 2, m + 3);
+    issue_tile<P, TE, KAHAN>(ba.shots[wt.x], wt.y & 0xFFFF, wt.y >> 16, stage0, bar0, m, m + 1, m + 2, m + 3);
   }
   for (int it = 0; w < ba.nitems; it++, w += gridDim.x) {
     const int s = it & 1;
@@ -572,13 +580,14 @@ persist_batch(const BatchArgs ba)
           fence_proxy_async();
           const int2 wnt = ba.items[wn];
           const CUtensorMap *m = ba.maps + 4 * wnt.x;
-          issue_tile<P, TE, KAHAN>(ba.shots[wnt.x], wnt.y, s ? stage0 : stage1, s ? bar0 : bar1, m, m + 1, m + 2, m + 3);
+          issue_tile<P, TE, KAHAN>(ba.shots[wnt.x], wnt.y & 0xFFFF, wnt.y >> 16, s ? stage0 : stage1, s ? bar0 : bar1, m,
+                                   m + 1, m + 2, m + 3);
         }
       }
     }
     __syncthreads();
-    if (!tile_body<P, TE, NT, KAHAN>(sp, wt.y, s ? stage1 : stage0, bar, parity, X1, X2, item, el, j, ecx, ecy, Dcj,
-                                     wj)) {
+    if (!tile_body<P, TE, NT, KAHAN>(sp, wt.y & 0xFFFF, wt.y >> 16, s ? stage1 : stage0, bar, parity, X1, X2, item, el,
+                                     j, ecx, ecy, Dcj, wj)) {
       if (threadIdx.x == 0) {
         atomicExch(ba.err, 1);
         mbar_wait_bounded(bar, parity);

@@ -41,7 +41,7 @@ struct Params {
 struct BatchArgs {
   const Params *shots;         // per shot, for this step's input buffer
   const CUtensorMap *maps;     // [shot][4]: region u, region cu, owned w, owned cw of the input buffers
-  const int2 *items;           // (shot, tile) work list
+  const int2 *items;           // (shot, ty << 16 | tx) work list of tile coordinates
   int nshots, nitems;
   int kblk;                    // step index within the block
   int write_a;                 // store a_k (last step of a block)

@@ -90,14 +90,31 @@ __global__ void k_gelu_bwd(const bf16 *dpost, const bf16 *pre, bf16 *dpre, long 
     dpre[i] = __float2bfloat16(__bfloat162float(dpost[i]) * nnk::gelu_grad_f(__bfloat162float(pre[i])));
 }
 
-// column sums of X[M][N] (bf16): partial[chunk][N] over rows [chunk*rows, ...)
+// column sums of X[M][N] (bf16): partial[chunk][N] over rows [chunk*rows, ...).  With N <= EW
+// the block's threads split into EW / N row lanes per column; each lane sums every
+// (EW / N)-th row of the chunk and the lanes are added in lane order (fixed partition).
 __global__ void k_colsum_partial(const bf16 *X, long M, int N, long rows, float *partial)
 {
+  __shared__ float s[EW];
   const long r0 = blockIdx.y * rows, r1 = (r0 + rows < M) ? r0 + rows : M;
-  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
-    float s = 0.f;
-    for (long r = r0; r < r1; r++) s += __bfloat162float(X[r * N + n]);
-    partial[(long)blockIdx.y * N + n] = s;
+  if (N <= EW) {
+    const int lanes = EW / N, c = threadIdx.x % N, lane = threadIdx.x / N;
+    float v = 0.f;
+    if (lane < lanes)
+      for (long r = r0 + lane; r < r1; r += lanes) v += __bfloat162float(X[r * N + c]);
+    s[threadIdx.x] = v;
+    __syncthreads();
+    if ((int)threadIdx.x < N) {
+      float t = 0.f;
+      for (int l = 0; l < lanes; l++) t += s[l * N + threadIdx.x];
+      partial[(long)blockIdx.y * N + threadIdx.x] = t;
+    }
+    return;
+  }
+  for (int n = threadIdx.x; n < N; n += blockDim.x) {
+    float t = 0.f;
+    for (long r = r0; r < r1; r++) t += __bfloat162float(X[r * N + n]);
+    partial[(long)blockIdx.y * N + n] = t;
   }
 }
 
@@ -373,7 +390,7 @@ cudaError_t launch_gemm(const GemmArgs &g, cudaStream_t st)
 int colsum(se2nn *h, const bf16 *X, long M, int N, long rows, float *out)
 {
   const int chunks = (int)((M + rows - 1) / rows);
-  k_colsum_partial<<<dim3(nblk(N), chunks), EW, 0, h->stream>>>(X, M, N, rows, h->partial);
+  k_colsum_partial<<<dim3(1, chunks), EW, 0, h->stream>>>(X, M, N, rows, h->partial);
   k_sum_parts<<<nblk(N), EW, 0, h->stream>>>(h->partial, chunks, N, out);
   NCK(h, cudaGetLastError());
   return 0;
