@@ -205,7 +205,7 @@ __device__ void sample_rows(const Params &prm, const float *rbuf_in, double *tra
 template <int P, int TE, int NT, bool KAHAN>
 __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, const unsigned char *st, uint32_t bar,
                                           uint32_t parity, float2 *X1, float2 *X2, int item, int el, int j, int ecx,
-                                          int ecy, const float (&Dcj)[P + 1], float wj)
+                                          int ecy, float wj)
 {
   typedef Geo<P, TE> G;
   typedef Layout<P, TE, KAHAN> L;
@@ -296,7 +296,6 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
   __syncthreads();
 
   // ---- 2. stress at the row's points; xi divergence; eta fluxes to X2 ---
-  float2 R[N1];
   if (active) {
     const float c11 = fmaf(2.f, mu, lam);
     const float nfj = -(detJ * wj);
@@ -311,27 +310,29 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
       Fxi[q] = make_float2(fx_ * sxx, fx_ * sxy);
       X2[el * NPE + q + j * N1] = make_float2(fy_ * sxy, fy_ * syy);
     }
+    // xi part of the divergence for the row's nodes, to X1 (this thread alone read row j of X1)
 #pragma unroll
     for (int a = 0; a < N1; a++) {
       float rx = 0.f, ry = 0.f;
 #pragma unroll
       for (int q = 0; q < N1; q++) { rx = fmaf(D[q * N1 + a], Fxi[q].x, rx); ry = fmaf(D[q * N1 + a], Fxi[q].y, ry); }
-      R[a] = make_float2(rx, ry);
+      X1[el * NPE + a + j * N1] = make_float2(rx, ry);
     }
   }
   __syncthreads();
 
-  // ---- 3. eta divergence for the row's nodes; element forces to X1 -----
+  // ---- 3. eta part of the divergence along column j (its 5 fluxes), added to X1 -----
   if (active) {
+    float2 fc[N1];
 #pragma unroll
-    for (int a = 0; a < N1; a++) {
-      float cx = R[a].x, cy = R[a].y;
+    for (int q = 0; q < N1; q++) fc[q] = X2[el * NPE + j + q * N1];
 #pragma unroll
-      for (int q = 0; q < N1; q++) {
-        const float2 f = X2[el * NPE + a + q * N1];
-        cx = fmaf(Dcj[q], f.x, cx); cy = fmaf(Dcj[q], f.y, cy);
-      }
-      X1[el * NPE + a + j * N1] = make_float2(cx, cy);
+    for (int bq = 0; bq < N1; bq++) {
+      const float2 r = X1[el * NPE + j + bq * N1];
+      float cx = r.x, cy = r.y;
+#pragma unroll
+      for (int q = 0; q < N1; q++) { cx = fmaf(D[q * N1 + bq], fc[q].x, cx); cy = fmaf(D[q * N1 + bq], fc[q].y, cy); }
+      X1[el * NPE + j + bq * N1] = make_float2(cx, cy);
     }
   }
   __syncthreads();
@@ -440,7 +441,6 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
   typedef Layout<P, TE, KAHAN> L;
   constexpr int N1 = G::N1, NEX = G::NEX;
   static_assert(NT >= G::ITEMS, "one (element, line) item per thread");
-  const float *D = c_D[P - 1];
   const float *W = c_w[P - 1];
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char *stage0 = smem;
@@ -464,9 +464,6 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
   const int item = threadIdx.x;
   const int el = item / N1, j = item - (item / N1) * N1;
   const int ecy = el / NEX, ecx = el - (el / NEX) * NEX;
-  float Dcj[N1];   // column j of D
-#pragma unroll
-  for (int k = 0; k < N1; k++) Dcj[k] = (item < G::ITEMS) ? D[k * N1 + j] : 0.f;
   const float wj = (item < G::ITEMS) ? W[j] : 0.f;
 
   // tile coordinates advance by the grid size without a division per tile
@@ -486,7 +483,7 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
       fence_proxy_async();
       issue_tile<P, TE, KAHAN>(prm, txn, tyn, s ? stage0 : stage1, s ? bar0 : bar1, &tm_u, &tm_cu, &tm_w, &tm_cw);
     }
-    if (!tile_body<P, TE, NT, KAHAN>(prm, tx, ty, s ? stage1 : stage0, bar, parity, X1, X2, item, el, j, ecx, ecy, Dcj, wj)) {
+    if (!tile_body<P, TE, NT, KAHAN>(prm, tx, ty, s ? stage1 : stage0, bar, parity, X1, X2, item, el, j, ecx, ecy, wj)) {
       if (threadIdx.x == 0) {
         atomicExch(prm.err, 1);
         // let this CTA's copies in flight land before the shared memory is released
@@ -522,7 +519,6 @@ persist_batch(const BatchArgs ba)
   constexpr int N1 = G::N1, NEX = G::NEX;
   static_assert(NT >= G::ITEMS, "one (element, line) item per thread");
   static_assert(sizeof(Params) % 8 == 0, "Params copied in 8-byte words");
-  const float *D = c_D[P - 1];
   const float *W = c_w[P - 1];
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char *stage0 = smem;
@@ -549,9 +545,6 @@ persist_batch(const BatchArgs ba)
   const int item = threadIdx.x;
   const int el = item / N1, j = item - (item / N1) * N1;
   const int ecy = el / NEX, ecx = el - (el / NEX) * NEX;
-  float Dcj[N1];
-#pragma unroll
-  for (int k = 0; k < N1; k++) Dcj[k] = (item < G::ITEMS) ? D[k * N1 + j] : 0.f;
   const float wj = (item < G::ITEMS) ? W[j] : 0.f;
 
   int w = blockIdx.x;
@@ -587,7 +580,7 @@ persist_batch(const BatchArgs ba)
     }
     __syncthreads();
     if (!tile_body<P, TE, NT, KAHAN>(sp, wt.y & 0xFFFF, wt.y >> 16, s ? stage1 : stage0, bar, parity, X1, X2, item, el,
-                                     j, ecx, ecy, Dcj, wj)) {
+                                     j, ecx, ecy, wj)) {
       if (threadIdx.x == 0) {
         atomicExch(ba.err, 1);
         mbar_wait_bounded(bar, parity);
