@@ -10,10 +10,11 @@
 // write C in FP32 or BF16; Cin may alias C (in-place accumulation).
 //
 // Tiles: 64 x 64 x 32 per CTA, 4 warps of 32 x 32, each warp 2 x 4
-// mma.m16n8k16 (bf16 -> f32).  Both operands are staged in shared memory
-// k-contiguous ([m][k] and [n][k]) whatever their global layout, so a single
-// fragment path serves every transpose combination; global loads are 16-byte
-// vectors when the contiguous dimension and the pointers allow it.
+// mma.m16n8k16 (bf16 -> f32).  Operands keep their global layout in shared
+// memory, filled by a 3-stage pipeline of 16-byte cp.async copies (zero-filled
+// at the edges; element copies when the leading dimension or the base is not
+// 16-byte aligned); fragments are read with ldmatrix, transposing (.trans) for
+// operands whose contiguous dimension is m or n.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -41,7 +42,9 @@ struct GemmArgs {
   long ldaux, sAux;
 };
 
-constexpr int GBM = 64, GBN = 64, GBK = 32, GPAD = 8, GTHREADS = 128;
+constexpr int GBM = 64, GBN = 64, GBK = 32, GPAD = 8, GTHREADS = 128, GSTAGES = 3;
+// one stage of one operand: [64][32 + 8] (k contiguous) or [32][64 + 8] (m or n contiguous)
+constexpr int GSTAGE_ELEMS = (GBM * (GBK + GPAD) > GBK * (GBM + GPAD)) ? GBM * (GBK + GPAD) : GBK * (GBM + GPAD);
 
 __device__ __forceinline__ float gelu_f(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
 __device__ __forceinline__ float gelu_grad_f(float x)
@@ -60,70 +63,65 @@ __device__ __forceinline__ void mma_bf16(float *d, const uint32_t *a, const uint
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-// stage a ROWS x GBK tile of a k-contiguous-in-shared operand:
-// element (r, k) of the tile is X[(r0 + r) * ld_r + (k0 + k) * ld_k] in global memory,
-// with (ld_r, ld_k) = (ld, 1) when k is contiguous, (1, ld) when r is.
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void ldsm_x4(uint32_t *r, uint32_t addr, bool trans)
+{
+  if (trans)
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(addr));
+  else
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(addr));
+}
+
+// 16-byte asynchronous copy global -> shared; bytes < 16 zero-fills the rest (0: nothing is read)
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src, int bytes)
+{
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_stages() { asm volatile("cp.async.wait_group %0;" ::"n"(GSTAGES - 2) : "memory"); }
+
+// Stage the k-tile starting at k0 of one operand, keeping its global layout:
+//   k contiguous (kc): tile [ROWS (m or n)][GBK], element (r, k) at X[(r0 + r) * ld + k0 + k];
+//   otherwise:         tile [GBK][ROWS],         element (k, r) at X[(k0 + k) * ld + r0 + r].
+// vec: 16-byte cp.async copies (ld % 8 == 0, 16-byte aligned base); else plain element copies.
 template <int ROWS>
-__device__ __forceinline__ void stage_tile(bf16 (*s)[GBK + GPAD], const bf16 *X, long ld, bool k_contig, int r0,
-                                           int rows, int k0, int K, bool vec_ok)
+__device__ __forceinline__ void stage_operand(bf16 *sm, const bf16 *X, long ld, bool kc, int r0, int rows, int k0,
+                                              int K, bool vec)
 {
   const bf16 zero = __float2bfloat16(0.f);
-  if (k_contig) {
-    if (vec_ok) {
-      // 8 consecutive k per 16-byte vector: ROWS * GBK / 8 vectors
-      for (int e = threadIdx.x; e < ROWS * GBK / 8; e += GTHREADS) {
-        const int r = e / (GBK / 8), kk = (e % (GBK / 8)) * 8;
-        const int gr = r0 + r, gk = k0 + kk;
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (gr < rows && gk + 7 < K) v = *reinterpret_cast<const uint4 *>(X + (long)gr * ld + gk);
-        else if (gr < rows) {
-          __align__(16) bf16 t[8];
-          for (int i = 0; i < 8; i++) t[i] = (gk + i < K) ? X[(long)gr * ld + gk + i] : zero;
-          v = *reinterpret_cast<uint4 *>(t);
-        }
-        *reinterpret_cast<uint4 *>(&s[r][kk]) = v;
-      }
-    } else {
-      for (int e = threadIdx.x; e < ROWS * GBK; e += GTHREADS) {
-        const int r = e / GBK, k = e % GBK;
-        const int gr = r0 + r, gk = k0 + k;
-        s[r][k] = (gr < rows && gk < K) ? X[(long)gr * ld + gk] : zero;
-      }
+  const int W = kc ? GBK : ROWS;            // tile row length (elements)
+  const int H = kc ? ROWS : GBK;            // tile rows
+  const int lim_row = kc ? rows - r0 : K - k0;     // valid tile rows
+  const int lim_col = kc ? K - k0 : rows - r0;     // valid elements per tile row
+  const long grow0 = kc ? r0 : k0, gcol0 = kc ? k0 : r0;
+  if (vec) {
+    for (int e = threadIdx.x; e < H * W / 8; e += GTHREADS) {
+      const int tr = e / (W / 8), tc = (e % (W / 8)) * 8;
+      int valid = (tr < lim_row) ? lim_col - tc : 0;
+      valid = valid < 0 ? 0 : (valid > 8 ? 8 : valid);
+      const bf16 *src = valid ? X + (grow0 + tr) * ld + gcol0 + tc : X;
+      cp_async16(smem_addr(sm + tr * (W + GPAD) + tc), src, valid * 2);
     }
   } else {
-    if (vec_ok) {
-      // 8 consecutive rows per 16-byte vector, transposed into shared memory
-      for (int e = threadIdx.x; e < ROWS * GBK / 8; e += GTHREADS) {
-        const int k = e / (ROWS / 8), rr = (e % (ROWS / 8)) * 8;
-        const int gk = k0 + k, gr = r0 + rr;
-        __align__(16) bf16 t[8];
-        if (gk < K && gr + 7 < rows) {
-          *reinterpret_cast<uint4 *>(t) = *reinterpret_cast<const uint4 *>(X + (long)gk * ld + gr);
-        } else {
-          for (int i = 0; i < 8; i++) t[i] = (gk < K && gr + i < rows) ? X[(long)gk * ld + gr + i] : zero;
-        }
-        for (int i = 0; i < 8; i++) s[rr + i][k] = t[i];
-      }
-    } else {
-      for (int e = threadIdx.x; e < ROWS * GBK; e += GTHREADS) {
-        const int k = e / ROWS, r = e % ROWS;
-        const int gr = r0 + r, gk = k0 + k;
-        s[r][k] = (gr < rows && gk < K) ? X[(long)gk * ld + gr] : zero;
-      }
+    for (int e = threadIdx.x; e < H * W; e += GTHREADS) {
+      const int tr = e / W, tc = e % W;
+      sm[tr * (W + GPAD) + tc] = (tr < lim_row && tc < lim_col) ? X[(grow0 + tr) * ld + gcol0 + tc] : zero;
     }
   }
 }
 
 __global__ void __launch_bounds__(GTHREADS) gemm_bf16(const GemmArgs g)
 {
-  __shared__ __align__(16) bf16 sA[GBM][GBK + GPAD];
-  __shared__ __align__(16) bf16 sB[GBN][GBK + GPAD];
+  __shared__ __align__(128) bf16 sA[GSTAGES][GSTAGE_ELEMS];
+  __shared__ __align__(128) bf16 sB[GSTAGES][GSTAGE_ELEMS];
   const int b = blockIdx.z;
   const int m0 = blockIdx.y * GBM, n0 = blockIdx.x * GBN;
   const bf16 *A = g.A + (long)b * g.sA;
   const bf16 *B = g.B + (long)b * g.sB;
-  // A as rows m: k contiguous unless transposed; B as rows n: k contiguous when transposed
-  const bool a_kc = !g.transA, b_kc = g.transB;
+  const bool a_kc = !g.transA, b_kc = g.transB;   // k contiguous in the stored tile
   const bool a_vec = ((g.lda % 8) == 0) && ((reinterpret_cast<uintptr_t>(A) & 15) == 0);
   const bool b_vec = ((g.ldb % 8) == 0) && ((reinterpret_cast<uintptr_t>(B) & 15) == 0);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -137,34 +135,59 @@ __global__ void __launch_bounds__(GTHREADS) gemm_bf16(const GemmArgs g)
 #pragma unroll
       for (int r = 0; r < 4; r++) acc[i][j][r] = 0.f;
 
-  for (int k0 = 0; k0 < g.K; k0 += GBK) {
-    stage_tile<GBM>(sA, A, g.lda, a_kc, m0, g.M, k0, g.K, a_vec);
-    stage_tile<GBN>(sB, B, g.ldb, b_kc, n0, g.N, k0, g.K, b_vec);
+  const int KT = (g.K + GBK - 1) / GBK;
+#pragma unroll
+  for (int st = 0; st < GSTAGES - 1; st++) {
+    if (st < KT) {
+      stage_operand<GBM>(sA[st], A, g.lda, a_kc, m0, g.M, st * GBK, g.K, a_vec);
+      stage_operand<GBN>(sB[st], B, g.ldb, b_kc, n0, g.N, st * GBK, g.K, b_vec);
+    }
+    cp_async_commit();
+  }
+  // ldmatrix row addresses: lane l -> matrix l / 8, row l % 8 of that 8x8 matrix
+  const int mat = lane >> 3, mrow = lane & 7;
+  for (int kt = 0; kt < KT; kt++) {
+    cp_async_wait_stages();
     __syncthreads();
+    {
+      const int nk = kt + GSTAGES - 1;
+      if (nk < KT) {
+        stage_operand<GBM>(sA[nk % GSTAGES], A, g.lda, a_kc, m0, g.M, nk * GBK, g.K, a_vec);
+        stage_operand<GBN>(sB[nk % GSTAGES], B, g.ldb, b_kc, n0, g.N, nk * GBK, g.K, b_vec);
+      }
+      cp_async_commit();
+    }
+    const bf16 *tA = sA[kt % GSTAGES];
+    const bf16 *tB = sB[kt % GSTAGES];
 #pragma unroll
     for (int kk = 0; kk < GBK; kk += 16) {
       uint32_t af[2][4], bfr[4][2];
 #pragma unroll
       for (int i = 0; i < 2; i++) {
-        const int r = wm + i * 16 + gid;
-        af[i][0] = *reinterpret_cast<const uint32_t *>(&sA[r][kk + tig * 2]);
-        af[i][1] = *reinterpret_cast<const uint32_t *>(&sA[r + 8][kk + tig * 2]);
-        af[i][2] = *reinterpret_cast<const uint32_t *>(&sA[r][kk + 8 + tig * 2]);
-        af[i][3] = *reinterpret_cast<const uint32_t *>(&sA[r + 8][kk + 8 + tig * 2]);
+        // matrices: 0 rows m..m+7 / k..k+7, 1 rows m+8.. / k.., 2 rows m.. / k+8.., 3 rows m+8.. / k+8..
+        const int mm = wm + i * 16 + (mat & 1) * 8, kq = kk + (mat >> 1) * 8;
+        const uint32_t addr = a_kc ? smem_addr(tA + (mm + mrow) * (GBK + GPAD) + kq)
+                                   : smem_addr(tA + (kq + mrow) * (GBM + GPAD) + mm);
+        ldsm_x4(af[i], addr, !a_kc);
       }
 #pragma unroll
-      for (int j = 0; j < 4; j++) {
-        const int c = wn + j * 8 + gid;
-        bfr[j][0] = *reinterpret_cast<const uint32_t *>(&sB[c][kk + tig * 2]);
-        bfr[j][1] = *reinterpret_cast<const uint32_t *>(&sB[c][kk + 8 + tig * 2]);
+      for (int jj = 0; jj < 2; jj++) {
+        // matrices: 0 n..n+7 / k..k+7, 1 n.. / k+8.., 2 n+8.. / k.., 3 n+8.. / k+8..
+        const int nn = wn + jj * 16 + (mat >> 1) * 8, kq = kk + (mat & 1) * 8;
+        const uint32_t addr = b_kc ? smem_addr(tB + (nn + mrow) * (GBK + GPAD) + kq)
+                                   : smem_addr(tB + (kq + mrow) * (GBN + GPAD) + nn);
+        uint32_t r[4];
+        ldsm_x4(r, addr, !b_kc);
+        bfr[2 * jj][0] = r[0]; bfr[2 * jj][1] = r[1];
+        bfr[2 * jj + 1][0] = r[2]; bfr[2 * jj + 1][1] = r[3];
       }
 #pragma unroll
       for (int i = 0; i < 2; i++)
 #pragma unroll
         for (int j = 0; j < 4; j++) mma_bf16(acc[i][j], af[i], bfr[j]);
     }
-    __syncthreads();
   }
+  asm volatile("cp.async.wait_all;" ::: "memory");
 
   // epilogue: accumulator element r of tile (i, j) is (row gid + 8*(r/2), column 2*tig + r%2);
   // the two columns of a row are handled as a pair (one 4- or 8-byte access) when aligned
