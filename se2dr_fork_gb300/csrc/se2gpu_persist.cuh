@@ -228,10 +228,25 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
   }
   const int s0 = prm.tile_src_off[t], s1 = prm.tile_src_off[t + 1];
   const int r0 = prm.tile_rec_off[t], r1 = prm.tile_rec_off[t + 1];
-  constexpr int MAXP = (G::NPAIR + NT - 1) / NT;
+  // node phase granularity: pairs of adjacent nodes (16-byte accesses), or single nodes strided
+  // by NT (8-byte accesses, still coalesced) when that lowers the most nodes any thread handles
+  constexpr int NOWN = G::OWM * G::OWM;
+  constexpr bool SINGLE = ((NOWN + NT - 1) / NT) < 2 * ((G::NPAIR + NT - 1) / NT);
+  constexpr int MAXS = SINGLE ? (NOWN + NT - 1) / NT : 1;
+  constexpr int MAXP = SINGLE ? 1 : (G::NPAIR + NT - 1) / NT;
+  float minv_s[MAXS];
+#pragma unroll
+  for (int k = 0; k < MAXS; k++) {
+    minv_s[k] = 0.f;
+    if constexpr (SINGLE) {
+      const int o = threadIdx.x + k * NT, oy = o / G::OWM, ox = o - (o / G::OWM) * G::OWM;
+      if (o < NOWN && oy < b.OH && ox < b.OW) minv_s[k] = prm.minv[(size_t)(b.Y0 + oy) * prm.pitch + b.X0 + ox];
+    }
+  }
   float2 minv_pre[MAXP];
 #pragma unroll
   for (int k = 0; k < MAXP; k++) {
+    if constexpr (SINGLE) { minv_pre[k] = make_float2(0.f, 0.f); continue; }
     const int o = threadIdx.x + k * NT;
     const int oy = o / G::PW, px = o - (o / G::PW) * G::PW;
     const int XA = b.OXa + 2 * px, Y = b.Y0 + oy;
@@ -337,9 +352,65 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
   }
   __syncthreads();
 
-  // ---- owned nodes, two adjacent per thread: ordered element sum, sources, update
+  // ---- owned nodes: ordered element sum, sources, update
+  if constexpr (SINGLE) {
+#pragma unroll
+    for (int k = 0; k < MAXS; k++) {
+      const int o = threadIdx.x + k * NT, oy = o / G::OWM, ox = o - (o / G::OWM) * G::OWM;
+      if (o >= NOWN || oy >= b.OH || ox >= b.OW) continue;
+      const int X = b.X0 + ox, Y = b.Y0 + oy;
+      float fx = 0.f, fy = 0.f;
+      {
+        const int lx = X - b.EX0 * P, ly = Y - b.EY0 * P;
+        const int ex = lx / P, ey = ly / P, ix = lx - ex * P, iy = ly - ey * P;
+        const bool in_x = X < prm.mx * P, in_y = Y < prm.my * P;
+        const bool lft = (ix == 0) && (X > 0), bot = (iy == 0) && (Y > 0);
+        const int own = (ey * NEX + ex) * NPE + ix + iy * N1;
+        if (bot && lft) { const float2 fe = X1[own - NEX * NPE - NPE + P + P * N1]; fx += fe.x; fy += fe.y; }
+        if (bot && in_x) { const float2 fe = X1[own - NEX * NPE + P * N1]; fx += fe.x; fy += fe.y; }
+        if (lft && in_y) { const float2 fe = X1[own - NPE + P]; fx += fe.x; fy += fe.y; }
+        if (in_x && in_y) { const float2 fe = X1[own]; fx += fe.x; fy += fe.y; }
+      }
+      for (int q = s0; q < s1; q++) {
+        const int sidx = prm.tile_src_idx[q], se = prm.src_elem[sidx], sx = se % prm.mx, sy = se / prm.mx;
+        const int a = X - sx * P, bb = Y - sy * P;
+        if (a >= 0 && a <= P && bb >= 0 && bb <= P) {
+          const float val = (float)prm.stf[sidx];
+          const float *sv = prm.src_vals + (size_t)sidx * 2 * NPE + 2 * (a + bb * N1);
+          fx = fmaf(val, sv[0], fx); fy = fmaf(val, sv[1], fy);
+        }
+      }
+      const float2 acc = make_float2(fx * minv_s[k], fy * minv_s[k]);
+      const int ri = (Y - b.RYa) * BXW + (X - b.RXa);
+      const int oi = oy * OBW + (X - b.OXa);
+      float2 u = rU[ri], w = oW[oi];
+      float2 cu = KAHAN ? rCU[ri] : make_float2(0.f, 0.f), cw = KAHAN ? oCW[oi] : make_float2(0.f, 0.f);
+      for (int q = r0; q < r1; q++) {
+        const int r = prm.tile_rec_idx[q], re = prm.rec_elem[r], rx = re % prm.mx, ry = re / prm.mx;
+        const int a = X - rx * P, bb = Y - ry * P;
+        if (a >= 0 && a <= P && bb >= 0 && bb <= P) {
+          float *rb = prm.rbuf_out + ((size_t)r * NPE + a + bb * N1) * 6;
+          rb[0] = u.x; rb[1] = u.y; rb[2] = fmaf(prm.half_dt, acc.x, w.x); rb[3] = fmaf(prm.half_dt, acc.y, w.y);
+          rb[4] = acc.x; rb[5] = acc.y;
+        }
+      }
+      if (KAHAN) {
+        kahan_add(w.x, cw.x, prm.dt * acc.x); kahan_add(w.y, cw.y, prm.dt * acc.y);
+        kahan_add(u.x, cu.x, prm.dt * w.x); kahan_add(u.y, cu.y, prm.dt * w.y);
+      } else {
+        w.x = fmaf(prm.dt, acc.x, w.x); w.y = fmaf(prm.dt, acc.y, w.y);
+        u.x = fmaf(prm.dt, w.x, u.x); u.y = fmaf(prm.dt, w.y, u.y);
+      }
+      const size_t n = (size_t)Y * prm.pitch + X;
+      prm.u_out[n] = u;
+      prm.w_out[n] = w;
+      if (KAHAN) { prm.cu_out[n] = cu; prm.cw_out[n] = cw; }
+      if (prm.a_out) prm.a_out[n] = acc;
+    }
+  }
 #pragma unroll
   for (int k = 0; k < MAXP; k++) {
+    if constexpr (SINGLE) break;
     const int o = threadIdx.x + k * NT;
     if (o >= G::NPAIR) break;
     const int oy = o / G::PW, px = o - (o / G::PW) * G::PW;
