@@ -42,6 +42,13 @@ def peaks():
         return 6800.0, "fallback"
 
 
+# DRAM bytes per node and step of the step kernels as ncu measured them (dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch at 1024^2, degree 4, divided by its 16.79M nodes; the
+# kernel's traffic grows in proportion to the nodes, so it is scaled to the workload's node
+# count): profiles/persist_step_fp32kahan_grf1024.md, profiles/step_kernel_fp64_grf512.md
+MEASURED_TRAFFIC_PER_NODE = {"fp32_kahan": 1109.6e6 / 16785409}
+
+
 def alg_bytes_per_node(precision: str, ne: int, nnodes: int) -> float:
     """Algorithmic DRAM bytes per node per step (unique traffic only)."""
     cell = ne / nnodes
@@ -228,8 +235,12 @@ def run_ours(args, rank, world):
         achieved = b * nnodes / per / 1e9
         results[prec] = {"value": replica_value(dof, k, world, secs), "ms_per_step": 1e3 * per, "steps": k, "tile": tile,
                          "launches": launches, "clocks": clk.summary(),
-                         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                                      "frac": achieved / hbm, "traffic": None,
+                         "roofline": {"bound": "hbm" if prec != "fp64" else "fp64 pipe (HBM fraction shown)",
+                                      "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                                      "frac": achieved / hbm,
+                                      "traffic": (MEASURED_TRAFFIC_PER_NODE[prec] * nnodes
+                                                  if prec in MEASURED_TRAFFIC_PER_NODE and args.mx == 2048 else None),
+                                      "traffic_note": "ncu DRAM bytes per node at 1024^2 x nodes (bytes per launch)",
                                       "alg_bytes_per_node": b, "peak_kind": peak_kind}}
 
     # end to end through the C-ABI: create (upload from host) + K steps + traces read back + destroy
