@@ -350,6 +350,8 @@ def run_ensemble(args):
     torch.cuda.set_device(0)
     t0 = time.perf_counter()
     specs = S.ensemble(args.shots, seed=3)
+    if args.ens_degree > 0:   # the same shots, all at one degree (per-degree efficiency of the batch kernel)
+        specs = [sp.replace(p=args.ens_degree) for sp in specs]
     with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
         setups = list(ex.map(H.Setup, specs))
     t_setup = time.perf_counter() - t0
@@ -562,6 +564,7 @@ def main():
     ap.add_argument("--ensemble", action="store_true", help="batched ensemble of --shots shots instead of the headline run")
     ap.add_argument("--shots", type=int, default=256)
     ap.add_argument("--block", type=int, default=100, help="ensemble steps per CUDA graph")
+    ap.add_argument("--ens-degree", type=int, default=0, help="give every ensemble shot this degree (0: as drawn)")
     ap.add_argument("--surrogate", action="store_true", help="surrogate training + serving instead of the headline run")
     ap.add_argument("--train", type=int, default=4000, help="surrogate training draws")
     ap.add_argument("--test", type=int, default=500, help="surrogate held-out requests (+10%% out of distribution)")

@@ -128,8 +128,8 @@ struct Layout {
   static constexpr size_t XCH = al128(sizeof(float2) * G::NE * G::NPE);   // exchange buffer
   static constexpr size_t MISC = 64;
   static constexpr size_t TOTAL = 2 * STAGE + 2 * XCH + MISC;
-  // the batched kernel keeps the current tile's shot parameters after the barriers
-  static constexpr size_t BATCH_TOTAL = TOTAL + al128(sizeof(Params));
+  // the batched kernel keeps the shot parameters of the current and the next tile after the barriers
+  static constexpr size_t BATCH_TOTAL = TOTAL + 2 * al128(sizeof(Params));
   static constexpr uint32_t TX_BYTES =
       (uint32_t)((KAHAN ? 2 : 1) * (sizeof(float2) * G::BXW * G::BXH + sizeof(float2) * G::OBW * G::OBH));
 };
@@ -155,20 +155,24 @@ __device__ __forceinline__ TileBox tile_box(const Params &prm, int tx, int ty)
   return b;
 }
 
-// issue the copies of tile t into a stage
+// issue the copies of tile (tx, ty) into a stage.  The box origins depend only on the
+// tile coordinates (the same formulas as tile_box); boxes reaching past the mesh
+// read the tensor maps' zero fill.
 template <int P, int TE, bool KAHAN>
-__device__ __forceinline__ void issue_tile(const Params &prm, int tx, int ty, unsigned char *stage, uint32_t bar,
+__device__ __forceinline__ void issue_tile(int tx, int ty, unsigned char *stage, uint32_t bar,
                                            const CUtensorMap *tm_u, const CUtensorMap *tm_cu,
                                            const CUtensorMap *tm_w, const CUtensorMap *tm_cw)
 {
   typedef Layout<P, TE, KAHAN> L;
-  const TileBox b = tile_box<P, TE>(prm, tx, ty);
+  const int ex0 = tx * TE, ey0 = ty * TE;
+  const int RXa = (max(ex0 - 1, 0) * P) & ~1, RYa = max(ey0 - 1, 0) * P;
+  const int OXa = (ex0 * P) & ~1, Y0 = ey0 * P;
   mbar_expect_tx(bar, L::TX_BYTES);
   size_t o = 0;
-  tma_load_2d(smem_u32(stage + o), tm_u, b.RXa, b.RYa, bar); o += L::REG;
-  if (KAHAN) { tma_load_2d(smem_u32(stage + o), tm_cu, b.RXa, b.RYa, bar); o += L::REG; }
-  tma_load_2d(smem_u32(stage + o), tm_w, b.OXa, b.Y0, bar); o += L::OWN;
-  if (KAHAN) { tma_load_2d(smem_u32(stage + o), tm_cw, b.OXa, b.Y0, bar); }
+  tma_load_2d(smem_u32(stage + o), tm_u, RXa, RYa, bar); o += L::REG;
+  if (KAHAN) { tma_load_2d(smem_u32(stage + o), tm_cu, RXa, RYa, bar); o += L::REG; }
+  tma_load_2d(smem_u32(stage + o), tm_w, OXa, Y0, bar); o += L::OWN;
+  if (KAHAN) { tma_load_2d(smem_u32(stage + o), tm_cw, OXa, Y0, bar); }
 }
 
 __device__ __forceinline__ void kahan_add(float &s, float &c, float inc)
@@ -541,7 +545,7 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
   int t = blockIdx.x;
   int tx = t % prm.ntx, ty = t / prm.ntx;
   const int dtx = gridDim.x % prm.ntx, dty = gridDim.x / prm.ntx;
-  if (t < prm.ntiles && threadIdx.x == 0) issue_tile<P, TE, KAHAN>(prm, tx, ty, stage0, bar0, &tm_u, &tm_cu, &tm_w, &tm_cw);
+  if (t < prm.ntiles && threadIdx.x == 0) issue_tile<P, TE, KAHAN>(tx, ty, stage0, bar0, &tm_u, &tm_cu, &tm_w, &tm_cw);
   for (int it = 0; t < prm.ntiles; it++, t += gridDim.x) {
     const int s = it & 1;
     const uint32_t bar = s ? bar1 : bar0;
@@ -552,7 +556,7 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
     const int tn = t + gridDim.x;
     if (threadIdx.x == 0 && tn < prm.ntiles) {
       fence_proxy_async();
-      issue_tile<P, TE, KAHAN>(prm, txn, tyn, s ? stage0 : stage1, s ? bar0 : bar1, &tm_u, &tm_cu, &tm_w, &tm_cw);
+      issue_tile<P, TE, KAHAN>(txn, tyn, s ? stage0 : stage1, s ? bar0 : bar1, &tm_u, &tm_cu, &tm_w, &tm_cw);
     }
     if (!tile_body<P, TE, NT, KAHAN>(prm, tx, ty, s ? stage1 : stage0, bar, parity, X1, X2, item, el, j, ecx, ecy, wj)) {
       if (threadIdx.x == 0) {
@@ -581,6 +585,19 @@ __device__ __forceinline__ const float *batch_rbuf(const Params &sh, int kblk)
   return (kblk & 1) ? sh.rbuf_in : sh.rbuf_out;
 }
 
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// one warp copies a shot's parameters (16-byte pieces, one per lane) into shared memory, asynchronously
+__device__ __forceinline__ void copy_params_async(Params *dst, const Params *src)
+{
+  const int lane = threadIdx.x & 31;
+  if (lane < (int)(sizeof(Params) / 16))
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(reinterpret_cast<unsigned char *>(dst) + 16 * lane)),
+                 "l"(reinterpret_cast<const unsigned char *>(src) + 16 * lane)
+                 : "memory");
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
 template <int P, int TE, int NT, bool KAHAN>
 __global__ void __launch_bounds__(NT, ((2 * (Layout<P, TE, KAHAN>::BATCH_TOTAL + 1024) <= 233472) ? 2 : 1))
 persist_batch(const BatchArgs ba)
@@ -589,7 +606,7 @@ persist_batch(const BatchArgs ba)
   typedef Layout<P, TE, KAHAN> L;
   constexpr int N1 = G::N1, NEX = G::NEX;
   static_assert(NT >= G::ITEMS, "one (element, line) item per thread");
-  static_assert(sizeof(Params) % 8 == 0, "Params copied in 8-byte words");
+  static_assert(sizeof(Params) % 16 == 0 && sizeof(Params) / 16 <= 32, "Params copied in 16-byte pieces by one warp");
   const float *W = c_w[P - 1];
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char *stage0 = smem;
@@ -598,7 +615,9 @@ persist_batch(const BatchArgs ba)
   float2 *X2 = reinterpret_cast<float2 *>(smem + 2 * L::STAGE + L::XCH);
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * L::STAGE + 2 * L::XCH);
   const uint32_t bar0 = smem_u32(&bars[0]), bar1 = smem_u32(&bars[1]);
-  Params &sp = *reinterpret_cast<Params *>(smem + L::TOTAL);   // the current tile's shot, this step's pointers
+  // two slots for the shot parameters of the current and the next tile (this step's pointers patched in)
+  Params *slot0 = reinterpret_cast<Params *>(smem + L::TOTAL);
+  Params *slot1 = reinterpret_cast<Params *>(smem + L::TOTAL + al128(sizeof(Params)));
 
   if (threadIdx.x == 0) {
     mbar_init(bar0, 1);
@@ -618,40 +637,51 @@ persist_batch(const BatchArgs ba)
   const int ecy = el / NEX, ecx = el - (el / NEX) * NEX;
   const float wj = (item < G::ITEMS) ? W[j] : 0.f;
 
+  // Per-tile pipeline.  Every thread keeps the work items of this tile and the next
+  // in registers (the list entry two tiles ahead is loaded one tile early).  The
+  // next tile's shot parameters are copied into the other parameter slot with
+  // cp.async by warp 0 while this tile is computed, and its TMA copies are issued
+  // at the top of this tile, so no dependent global load sits between two tiles.
+  const int stride = gridDim.x;
   int w = blockIdx.x;
-  if (w < ba.nitems && threadIdx.x == 0) {
-    const int2 wt = ba.items[w];
-    const CUtensorMap *m = ba.maps + 4 * wt.x;
-    issue_tile<P, TE, KAHAN>(ba.shots[wt.x], wt.y & 0xFFFF, wt.y >> 16, stage0, bar0, m, m + 1, m + 2, m + 3);
+  int2 cur = make_int2(0, 0), nxt = make_int2(0, 0);
+  if (w < ba.nitems) cur = ba.items[w];
+  if (w + stride < ba.nitems) nxt = ba.items[w + stride];
+  if (w < ba.nitems) {
+    if (threadIdx.x == 0) {
+      const CUtensorMap *m = ba.maps + 4 * cur.x;
+      issue_tile<P, TE, KAHAN>(cur.y & 0xFFFF, cur.y >> 16, stage0, bar0, m, m + 1, m + 2, m + 3);
+    }
+    if (threadIdx.x < 32) copy_params_async(slot0, ba.shots + cur.x);
   }
-  for (int it = 0; w < ba.nitems; it++, w += gridDim.x) {
+  for (int it = 0; w < ba.nitems; it++, w += stride) {
     const int s = it & 1;
     const uint32_t bar = s ? bar1 : bar0;
     const uint32_t parity = (it >> 1) & 1;
-    const int wn = w + gridDim.x;
-    const int2 wt = ba.items[w];
+    const int wn = w + stride;
+    Params &sp = s ? *slot1 : *slot0;
+    const int2 nn = (wn + stride < ba.nitems) ? ba.items[wn + stride] : make_int2(0, 0);   // for the next tile
     if (threadIdx.x < 32) {
-      // warp 0 copies the shot's parameters and patches this step's pointers
-      const uint64_t *src = reinterpret_cast<const uint64_t *>(&ba.shots[wt.x]);
-      uint64_t *dst = reinterpret_cast<uint64_t *>(&sp);
-      for (int i = threadIdx.x; i < (int)(sizeof(Params) / 8); i += 32) dst[i] = src[i];
+      cp_async_wait_all();
       __syncwarp();
       if (threadIdx.x == 0) {
+        // this step's pointers of the tile's shot
         sp.stf = sp.stf + (size_t)ba.kblk * sp.nsrc;
-        sp.rbuf_out = const_cast<float *>(batch_rbuf(ba.shots[wt.x], ba.kblk));
+        sp.rbuf_out = const_cast<float *>(batch_rbuf(sp, ba.kblk));
         if (!ba.write_a) sp.a_out = nullptr;
         if (wn < ba.nitems) {
           fence_proxy_async();
-          const int2 wnt = ba.items[wn];
-          const CUtensorMap *m = ba.maps + 4 * wnt.x;
-          issue_tile<P, TE, KAHAN>(ba.shots[wnt.x], wnt.y & 0xFFFF, wnt.y >> 16, s ? stage0 : stage1, s ? bar0 : bar1, m,
-                                   m + 1, m + 2, m + 3);
+          const CUtensorMap *m = ba.maps + 4 * nxt.x;
+          issue_tile<P, TE, KAHAN>(nxt.y & 0xFFFF, nxt.y >> 16, s ? stage0 : stage1, s ? bar0 : bar1, m, m + 1,
+                                   m + 2, m + 3);
         }
       }
     }
-    __syncthreads();
-    if (!tile_body<P, TE, NT, KAHAN>(sp, wt.y & 0xFFFF, wt.y >> 16, s ? stage1 : stage0, bar, parity, X1, X2, item, el,
-                                     j, ecx, ecy, wj)) {
+    __syncthreads();   // slot s is complete; every thread has left the previous tile, so the other slot is free
+    if (threadIdx.x < 32 && wn < ba.nitems) copy_params_async(s ? slot0 : slot1, ba.shots + nxt.x);
+    if (!tile_body<P, TE, NT, KAHAN>(sp, cur.y & 0xFFFF, cur.y >> 16, s ? stage1 : stage0, bar, parity, X1, X2, item,
+                                     el, j, ecx, ecy, wj)) {
+      if (threadIdx.x < 32) cp_async_wait_all();
       if (threadIdx.x == 0) {
         atomicExch(ba.err, 1);
         mbar_wait_bounded(bar, parity);
@@ -659,6 +689,8 @@ persist_batch(const BatchArgs ba)
       }
       return;
     }
+    cur = nxt;
+    nxt = nn;
   }
 }
 
