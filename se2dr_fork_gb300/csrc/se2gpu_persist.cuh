@@ -356,6 +356,13 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
   }
   __syncthreads();
 
+  // the node phase's parameters in registers: when prm lives in shared memory (the
+  // batched kernel), every store through an output pointer would otherwise force
+  // the following parameter reads to be repeated
+  float2 *const u_out = prm.u_out, *const w_out = prm.w_out, *const cu_out = prm.cu_out, *const cw_out = prm.cw_out;
+  float2 *const a_out = prm.a_out;
+  const int pitch = prm.pitch, NXP = prm.mx * P, NYP = prm.my * P;
+  const float dt = prm.dt, half_dt = prm.half_dt;
   // ---- owned nodes: ordered element sum, sources, update
   if constexpr (SINGLE) {
 #pragma unroll
@@ -367,7 +374,7 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
       {
         const int lx = X - b.EX0 * P, ly = Y - b.EY0 * P;
         const int ex = lx / P, ey = ly / P, ix = lx - ex * P, iy = ly - ey * P;
-        const bool in_x = X < prm.mx * P, in_y = Y < prm.my * P;
+        const bool in_x = X < NXP, in_y = Y < NYP;
         const bool lft = (ix == 0) && (X > 0), bot = (iy == 0) && (Y > 0);
         const int own = (ey * NEX + ex) * NPE + ix + iy * N1;
         if (bot && lft) { const float2 fe = X1[own - NEX * NPE - NPE + P + P * N1]; fx += fe.x; fy += fe.y; }
@@ -394,22 +401,22 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
         const int a = X - rx * P, bb = Y - ry * P;
         if (a >= 0 && a <= P && bb >= 0 && bb <= P) {
           float *rb = prm.rbuf_out + ((size_t)r * NPE + a + bb * N1) * 6;
-          rb[0] = u.x; rb[1] = u.y; rb[2] = fmaf(prm.half_dt, acc.x, w.x); rb[3] = fmaf(prm.half_dt, acc.y, w.y);
+          rb[0] = u.x; rb[1] = u.y; rb[2] = fmaf(half_dt, acc.x, w.x); rb[3] = fmaf(half_dt, acc.y, w.y);
           rb[4] = acc.x; rb[5] = acc.y;
         }
       }
       if (KAHAN) {
-        kahan_add(w.x, cw.x, prm.dt * acc.x); kahan_add(w.y, cw.y, prm.dt * acc.y);
-        kahan_add(u.x, cu.x, prm.dt * w.x); kahan_add(u.y, cu.y, prm.dt * w.y);
+        kahan_add(w.x, cw.x, dt * acc.x); kahan_add(w.y, cw.y, dt * acc.y);
+        kahan_add(u.x, cu.x, dt * w.x); kahan_add(u.y, cu.y, dt * w.y);
       } else {
-        w.x = fmaf(prm.dt, acc.x, w.x); w.y = fmaf(prm.dt, acc.y, w.y);
-        u.x = fmaf(prm.dt, w.x, u.x); u.y = fmaf(prm.dt, w.y, u.y);
+        w.x = fmaf(dt, acc.x, w.x); w.y = fmaf(dt, acc.y, w.y);
+        u.x = fmaf(dt, w.x, u.x); u.y = fmaf(dt, w.y, u.y);
       }
-      const size_t n = (size_t)Y * prm.pitch + X;
-      prm.u_out[n] = u;
-      prm.w_out[n] = w;
-      if (KAHAN) { prm.cu_out[n] = cu; prm.cw_out[n] = cw; }
-      if (prm.a_out) prm.a_out[n] = acc;
+      const size_t n = (size_t)Y * pitch + X;
+      u_out[n] = u;
+      w_out[n] = w;
+      if (KAHAN) { cu_out[n] = cu; cw_out[n] = cw; }
+      if (a_out) a_out[n] = acc;
     }
   }
 #pragma unroll
@@ -431,7 +438,7 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
       // below, left, own), addressed relative to the node's own element in the region
       const int lx = X - b.EX0 * P, ly = Y - b.EY0 * P;
       const int ex = lx / P, ey = ly / P, ix = lx - ex * P, iy = ly - ey * P;
-      const bool in_x = X < prm.mx * P, in_y = Y < prm.my * P;
+      const bool in_x = X < NXP, in_y = Y < NYP;
       const bool lft = (ix == 0) && (X > 0), bot = (iy == 0) && (Y > 0);
       const int own = (ey * NEX + ex) * NPE + ix + iy * N1;
       if (bot && lft) { const float2 fe = X1[own - NEX * NPE - NPE + P + P * N1]; f[h][0] += fe.x; f[h][1] += fe.y; }
@@ -468,38 +475,38 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
           const int a = X - rx * P, bb = Y - ry * P;
           if (a >= 0 && a <= P && bb >= 0 && bb <= P) {
             float *rb = prm.rbuf_out + ((size_t)r * NPE + a + bb * N1) * 6;
-            rb[0] = ux; rb[1] = uy; rb[2] = fmaf(prm.half_dt, ax, wx); rb[3] = fmaf(prm.half_dt, ay, wy);
+            rb[0] = ux; rb[1] = uy; rb[2] = fmaf(half_dt, ax, wx); rb[3] = fmaf(half_dt, ay, wy);
             rb[4] = ax; rb[5] = ay;
           }
         }
       }
     }
     if (KAHAN) {
-      kahan_add(w.x, cw.x, prm.dt * acc.x); kahan_add(w.y, cw.y, prm.dt * acc.y);
-      kahan_add(w.z, cw.z, prm.dt * acc.z); kahan_add(w.w, cw.w, prm.dt * acc.w);
-      kahan_add(u.x, cu.x, prm.dt * w.x); kahan_add(u.y, cu.y, prm.dt * w.y);
-      kahan_add(u.z, cu.z, prm.dt * w.z); kahan_add(u.w, cu.w, prm.dt * w.w);
+      kahan_add(w.x, cw.x, dt * acc.x); kahan_add(w.y, cw.y, dt * acc.y);
+      kahan_add(w.z, cw.z, dt * acc.z); kahan_add(w.w, cw.w, dt * acc.w);
+      kahan_add(u.x, cu.x, dt * w.x); kahan_add(u.y, cu.y, dt * w.y);
+      kahan_add(u.z, cu.z, dt * w.z); kahan_add(u.w, cu.w, dt * w.w);
     } else {
-      w.x = fmaf(prm.dt, acc.x, w.x); w.y = fmaf(prm.dt, acc.y, w.y);
-      w.z = fmaf(prm.dt, acc.z, w.z); w.w = fmaf(prm.dt, acc.w, w.w);
-      u.x = fmaf(prm.dt, w.x, u.x); u.y = fmaf(prm.dt, w.y, u.y);
-      u.z = fmaf(prm.dt, w.z, u.z); u.w = fmaf(prm.dt, w.w, u.w);
+      w.x = fmaf(dt, acc.x, w.x); w.y = fmaf(dt, acc.y, w.y);
+      w.z = fmaf(dt, acc.z, w.z); w.w = fmaf(dt, acc.w, w.w);
+      u.x = fmaf(dt, w.x, u.x); u.y = fmaf(dt, w.y, u.y);
+      u.z = fmaf(dt, w.z, u.z); u.w = fmaf(dt, w.w, u.w);
     }
-    const size_t n = (size_t)Y * prm.pitch + XA;
+    const size_t n = (size_t)Y * pitch + XA;
     if (v0 && v1) {
-      *reinterpret_cast<float4 *>(prm.u_out + n) = u;
-      *reinterpret_cast<float4 *>(prm.w_out + n) = w;
-      if (KAHAN) { *reinterpret_cast<float4 *>(prm.cu_out + n) = cu; *reinterpret_cast<float4 *>(prm.cw_out + n) = cw; }
-      if (prm.a_out) *reinterpret_cast<float4 *>(prm.a_out + n) = acc;
+      *reinterpret_cast<float4 *>(u_out + n) = u;
+      *reinterpret_cast<float4 *>(w_out + n) = w;
+      if (KAHAN) { *reinterpret_cast<float4 *>(cu_out + n) = cu; *reinterpret_cast<float4 *>(cw_out + n) = cw; }
+      if (a_out) *reinterpret_cast<float4 *>(a_out + n) = acc;
     } else {
       const int h = v0 ? 0 : 1;
-      prm.u_out[n + h] = h ? make_float2(u.z, u.w) : make_float2(u.x, u.y);
-      prm.w_out[n + h] = h ? make_float2(w.z, w.w) : make_float2(w.x, w.y);
+      u_out[n + h] = h ? make_float2(u.z, u.w) : make_float2(u.x, u.y);
+      w_out[n + h] = h ? make_float2(w.z, w.w) : make_float2(w.x, w.y);
       if (KAHAN) {
-        prm.cu_out[n + h] = h ? make_float2(cu.z, cu.w) : make_float2(cu.x, cu.y);
-        prm.cw_out[n + h] = h ? make_float2(cw.z, cw.w) : make_float2(cw.x, cw.y);
+        cu_out[n + h] = h ? make_float2(cu.z, cu.w) : make_float2(cu.x, cu.y);
+        cw_out[n + h] = h ? make_float2(cw.z, cw.w) : make_float2(cw.x, cw.y);
       }
-      if (prm.a_out) prm.a_out[n + h] = h ? make_float2(acc.z, acc.w) : make_float2(acc.x, acc.y);
+      if (a_out) a_out[n + h] = h ? make_float2(acc.z, acc.w) : make_float2(acc.x, acc.y);
     }
   }
   __syncthreads();   // stage s and the exchange buffers are free again
