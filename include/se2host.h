@@ -50,6 +50,10 @@ typedef struct se2_spec {
      (ElastoDynamicsSetSourceImplementation / -source_impl, 2202-2266) */
   int src_impl;
   double sm_h;
+  /* interpolating receivers (RecordUV_interp, se2wave.c:2445-2581): displacement, velocity
+     and acceleration at the exact points, from the Lagrange interpolant of their element */
+  int ninterp;
+  const double *interp_xy;       /* ninterp*2 */
 } se2_spec;
 
 /* Everything the device needs, FP64, owned by the library. */
@@ -83,6 +87,15 @@ typedef struct se2_setup {
      nsrc_phys sources of the spec (src_owner); one entry per source unless src_impl >= 0 */
   int nsrc_phys;
   int *src_owner;
+  /* receiver list = the nrec_sta nearest-GLL stations of the spec, then, for each of the
+     ninterp interpolating receivers, the (p+1)^2 nodes k of its element interp_elem[i]
+     (entry nrec_sta + i*npe + k, gll index k); nrec = nrec_sta + ninterp*npe.
+     interp_N[i*npe + k] = N_k at the receiver, interp_xri = the interpolated coordinate */
+  int nrec_sta;
+  int ninterp;
+  double *interp_xy;
+  int *interp_elem;
+  double *interp_N, *interp_xri;
 } se2_setup;
 
 const char *se2_host_last_error(void);
@@ -99,6 +112,21 @@ int se2_gll(int p, double *xi, double *w);
 int se2_basis_1d(int p, int npoints, const double *x, double *N);
 /* TabulateBasisDerivatives1d_CLEGENDRE (387-523): dN[k*(p+1)+i] = dN_i/dxi(x_k) */
 int se2_basis_deriv_1d(int p, int npoints, const double *x, double *dN);
+
+/* Interpolating receiver (RecordUV_interp, se2wave.c:2445-2581): the containing element
+   ei = (int)((x - gmin.x)/dx), ej likewise with dx = (gmax - gmin)/mx (2494-2500), the
+   reference coordinates xi = 2(x - x0)/dx - 1 (2518-2519) and the tensor weights
+   N[i + j*(p+1)] = N_i(xi)*N_j(eta) of TabulateBasis1d_CLEGENDRE (2522-2531).  *eid =
+   ei + ej*mx; xri = sum_k N_k * (node coordinates) (2535-2541), the coordinate the reference
+   prints.  Points outside [gmin, gmax) are rejected (the reference does not check; at
+   x = gmax its element index runs past the mesh). */
+int se2_interp_receiver(const se2_setup *s, const double xy[2], int *eid, double *N, double xri[2]);
+/* Values at the interpolating receivers from receiver rows of the device library
+   (rows[j][7*nrec], the se2gpu_traces layout over the setup's receiver list):
+   out[j][7*i + c] = sum_k N_k rows[j][7*(nrec_sta + i*npe + k) + c], k ascending as the
+   reference sums (2561-2569); c = ux uy vx vy ax ay curl(v).  The element's interpolant is
+   in Q_p, as is its curl, so the curl of the interpolant at the point is exact too. */
+int se2_interp_rows(const se2_setup *s, long nrows, const double *rows, double *out);
 
 /* Source-time function values (SeismicSTFEvaluate 3458-3466 with the Ricker,
    Gaussian and Yoffe evaluators).  For steps k = 1..n after time `*time`, the

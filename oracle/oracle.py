@@ -249,6 +249,11 @@ def ref_run(spec, extra_args=(), force_u: Optional[np.ndarray] = None) -> dict:
         if "trace_capture" in out:
             width = 1 + 7 * len(spec.receivers)
             out["traces"] = out["trace_capture"].reshape(-1, width)
+        if "interp_capture" in out:   # RecordUV_interp rows: time ux uy vx vy
+            out["interp"] = out["interp_capture"].reshape(-1, 5)
+            for line in r.stdout.splitlines():   # its first call prints the interpolated coordinate
+                if "interpolated coordinate" in line:
+                    out["interp_xri_text"] = np.array([float(t) for t in line.split("-->")[1].split()])
         return out
 
 

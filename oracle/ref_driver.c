@@ -17,8 +17,9 @@
  *       the reference's STF evaluators (se2wave.c:3500-3822) on a time grid
  *
  * Receiver values are captured from the reference's own fprintf calls inside
- * RecordUVA_MultipleStations_NearestGLL_MPI (se2wave.c:2908-2962) at full
- * double precision (the .dat text keeps only 9 significant digits).
+ * RecordUVA_MultipleStations_NearestGLL_MPI (se2wave.c:2908-2962) and, with
+ * the spec key "irec x y", RecordUV_interp (2445-2581) at full double
+ * precision (the .dat text keeps only 9 significant digits).
  */
 #include <petsc.h>
 #include <petsctime.h>
@@ -28,17 +29,19 @@
 #include <stdarg.h>
 
 /* ---- fprintf capture ---------------------------------------------- */
-static int     cap_on = 0;
-static double *cap_buf = NULL;
-static size_t  cap_n = 0, cap_cap = 0;
+/* two capture buffers: [0] the multi-station recorder, [1] RecordUV_interp */
+static int     cap_on = 0, cap_sel = 0;
+static double *cap_buf[2] = {NULL, NULL};
+static size_t  cap_n[2] = {0, 0}, cap_cap[2] = {0, 0};
 
 static void cap_push(double v)
 {
-  if (cap_n == cap_cap) {
-    cap_cap = cap_cap ? 2 * cap_cap : 4096;
-    cap_buf = (double*)realloc(cap_buf, cap_cap * sizeof(double));
+  const int b = cap_sel;
+  if (cap_n[b] == cap_cap[b]) {
+    cap_cap[b] = cap_cap[b] ? 2 * cap_cap[b] : 4096;
+    cap_buf[b] = (double*)realloc(cap_buf[b], cap_cap[b] * sizeof(double));
   }
-  cap_buf[cap_n++] = v;
+  cap_buf[b][cap_n[b]++] = v;
 }
 
 int se2lite_fprintf(FILE *fp, const char *fmt, ...)
@@ -89,6 +92,8 @@ typedef struct {
   double rec_xy[2 * MAXR];
   int perturb;
   double dvp, dvs, drho;
+  int irec;                    /* one interpolating receiver (RecordUV_interp keeps one per process) */
+  double irec_xy[2];
 } Spec;
 
 static int read_spec(const char *fname, Spec *sp)
@@ -112,6 +117,7 @@ static int read_spec(const char *fname, Spec *sp)
     else if (!strcmp(key, "rho")) fscanf(f, "%lf", &sp->rho);
     else if (!strcmp(key, "cell_file")) fscanf(f, "%1023s", sp->cell_file);
     else if (!strcmp(key, "cfl")) fscanf(f, "%lf", &sp->cfl);
+    else if (!strcmp(key, "irec")) { sp->irec = 1; fscanf(f, "%lf %lf", &sp->irec_xy[0], &sp->irec_xy[1]); }
     else if (!strcmp(key, "perturb")) { sp->perturb = 1; fscanf(f, "%lf %lf %lf", &sp->dvp, &sp->dvs, &sp->drho); }
     else if (!strcmp(key, "dt")) fscanf(f, "%lf", &sp->dt);
     else if (!strcmp(key, "tmax")) fscanf(f, "%lf", &sp->tmax);
@@ -321,6 +327,13 @@ static PetscErrorCode run(const Spec *sp, const char *outdir)
     if (!ignore_receiver_output && sp->nrec > 0) {
       ierr = RecordUVA_MultipleStations_NearestGLL(ctx, time, sp->nrec, (PetscReal*)sp->rec_xy, u, v, a); CHKERRQ(ierr);
     }
+    if (sp->irec) {
+      PetscReal xr[2];
+      xr[0] = sp->irec_xy[0]; xr[1] = sp->irec_xy[1];
+      cap_sel = 1;
+      ierr = RecordUV_interp(ctx, time, xr, u, v); CHKERRQ(ierr);
+      cap_sel = 0;
+    }
     if (time >= time_max) break;
   }
   cap_on = 0;
@@ -330,7 +343,8 @@ static PetscErrorCode run(const Spec *sp, const char *outdir)
     meta[0] = dt; meta[1] = time; meta[2] = (double)nsteps; meta[3] = (double)nt;
     dump(outdir, "run_meta.bin", meta, sizeof(meta));
   }
-  dump(outdir, "trace_capture.bin", cap_buf, sizeof(double) * cap_n);
+  dump(outdir, "trace_capture.bin", cap_buf[0], sizeof(double) * cap_n[0]);
+  if (sp->irec) dump(outdir, "interp_capture.bin", cap_buf[1], sizeof(double) * cap_n[1]);
   dump(outdir, "u.bin", u->array, sizeof(double) * u->n);
   dump(outdir, "v.bin", v->array, sizeof(double) * v->n);
   dump(outdir, "a.bin", a->array, sizeof(double) * a->n);

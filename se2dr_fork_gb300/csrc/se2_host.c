@@ -463,6 +463,7 @@ void se2_setup_destroy(se2_setup *s)
   free(s->mass); free(s->src_elem); free(s->src_gll); free(s->src_vals); free(s->stf_type); free(s->stf_par);
   free(s->src_owner);
   free(s->rec_xy); free(s->rec_node); free(s->rec_elem); free(s->rec_gll);
+  free(s->interp_xy); free(s->interp_elem); free(s->interp_N); free(s->interp_xri);
   free(s);
 }
 
@@ -689,6 +690,55 @@ static int locate_receiver(se2_setup *s, int r)
   return 0;
 }
 
+int se2_interp_receiver(const se2_setup *s, const double xy[2], int *eid, double *N, double xri[2])
+{
+  double gmin[2], gmax[2], dx, dy, x0, y0, xi, eta, Ns1[17], Ns2[17], xr0 = 0.0, xr1 = 0.0;
+  int ei, ej, i, j, k;
+  if (!s || !xy || !eid || !N || !xri) SE2_FAIL("null argument");
+  gmin[0] = s->gmin[0]; gmin[1] = s->gmin[1]; gmax[0] = s->gmax[0]; gmax[1] = s->gmax[1];
+  if (!(xy[0] >= gmin[0] && xy[0] < gmax[0] && xy[1] >= gmin[1] && xy[1] < gmax[1]))
+    SE2_FAIL("interpolating receiver (%+1.8e, %+1.8e) outside [gmin, gmax) of the mesh", xy[0], xy[1]);
+  dx = (gmax[0] - gmin[0]) / ((double)s->mx);
+  ei = (int)((xy[0] - gmin[0]) / dx);
+  dy = (gmax[1] - gmin[1]) / ((double)s->my);
+  ej = (int)((xy[1] - gmin[1]) / dy);
+  if (ei < 0 || ej < 0 || ei >= s->mx || ej >= s->my)
+    SE2_FAIL("interpolating receiver (%+1.8e, %+1.8e): element (%d, %d) outside the mesh", xy[0], xy[1], ei, ej);
+  x0 = gmin[0] + ei * dx;
+  y0 = gmin[1] + ej * dy;
+  xi = 2.0 * (xy[0] - x0) / dx - 1.0;
+  eta = 2.0 * (xy[1] - y0) / dy - 1.0;
+  if (se2_basis_1d(s->p, 1, &xi, Ns1) || se2_basis_1d(s->p, 1, &eta, Ns2)) return -1;
+  k = 0;
+  for (j = 0; j < s->n1; j++)
+    for (i = 0; i < s->n1; i++) { N[k] = Ns1[i] * Ns2[j]; k++; }
+  for (k = 0; k < s->npe; k++) {
+    const int gi = ei * s->p + k % s->n1, gj = ej * s->p + k / s->n1;
+    xr0 += N[k] * s->xnode[gi];
+    xr1 += N[k] * s->ynode[gj];
+  }
+  *eid = ei + ej * s->mx;
+  xri[0] = xr0; xri[1] = xr1;
+  return 0;
+}
+
+int se2_interp_rows(const se2_setup *s, long nrows, const double *rows, double *out)
+{
+  long j;
+  int i, k, c;
+  if (!s || nrows < 0 || (nrows > 0 && s->ninterp > 0 && (!rows || !out))) SE2_FAIL("null argument");
+  for (j = 0; j < nrows; j++)
+    for (i = 0; i < s->ninterp; i++) {
+      const double *Ni = s->interp_N + (size_t)i * s->npe;
+      for (c = 0; c < 7; c++) {
+        double v = 0.0;
+        for (k = 0; k < s->npe; k++) v += Ni[k] * rows[(size_t)j * 7 * s->nrec + 7 * ((size_t)s->nrec_sta + (size_t)i * s->npe + k) + c];
+        out[(size_t)j * 7 * s->ninterp + 7 * i + c] = v;
+      }
+    }
+  return 0;
+}
+
 int se2_setup_create(const se2_spec *sp, se2_setup **out)
 {
   se2_setup *s;
@@ -878,14 +928,39 @@ int se2_setup_create(const se2_spec *sp, se2_setup **out)
     free(g); free(taken);
   }
 
-  /* receivers */
-  s->nrec = sp->nrec;
-  s->rec_xy = (double*)xcalloc((size_t)sp->nrec * 2, sizeof(double));
-  s->rec_node = (int*)xcalloc((size_t)sp->nrec, sizeof(int));
-  s->rec_elem = (int*)xcalloc((size_t)sp->nrec, sizeof(int));
-  s->rec_gll = (int*)xcalloc((size_t)sp->nrec, sizeof(int));
+  /* receivers: the nearest-GLL stations, then the element nodes of each interpolating receiver */
+  if (sp->ninterp < 0 || (sp->ninterp > 0 && !sp->interp_xy)) { se2_setup_destroy(s); SE2_FAIL("bad interpolating receiver list"); }
+  s->nrec_sta = sp->nrec;
+  s->ninterp = sp->ninterp;
+  s->nrec = sp->nrec + sp->ninterp * s->npe;
+  s->rec_xy = (double*)xcalloc((size_t)s->nrec * 2, sizeof(double));
+  s->rec_node = (int*)xcalloc((size_t)s->nrec, sizeof(int));
+  s->rec_elem = (int*)xcalloc((size_t)s->nrec, sizeof(int));
+  s->rec_gll = (int*)xcalloc((size_t)s->nrec, sizeof(int));
+  s->interp_xy = (double*)xcalloc((size_t)sp->ninterp * 2, sizeof(double));
+  s->interp_elem = (int*)xcalloc((size_t)sp->ninterp, sizeof(int));
+  s->interp_N = (double*)xcalloc((size_t)sp->ninterp * s->npe, sizeof(double));
+  s->interp_xri = (double*)xcalloc((size_t)sp->ninterp * 2, sizeof(double));
   if (sp->nrec) memcpy(s->rec_xy, sp->rec_xy, sizeof(double) * 2 * sp->nrec);
   for (i = 0; i < sp->nrec; i++) if (locate_receiver(s, i)) { se2_setup_destroy(s); return -1; }
+  for (i = 0; i < sp->ninterp; i++) {
+    int k, eid;
+    s->interp_xy[2 * i] = sp->interp_xy[2 * i]; s->interp_xy[2 * i + 1] = sp->interp_xy[2 * i + 1];
+    if (se2_interp_receiver(s, &s->interp_xy[2 * i], &eid, &s->interp_N[(size_t)i * s->npe], &s->interp_xri[2 * i])) {
+      se2_setup_destroy(s);
+      return -1;
+    }
+    s->interp_elem[i] = eid;
+    for (k = 0; k < s->npe; k++) {
+      const int r = sp->nrec + i * s->npe + k;
+      const int gi = (eid % s->mx) * s->p + k % s->n1, gj = (eid / s->mx) * s->p + k / s->n1;
+      s->rec_elem[r] = eid;
+      s->rec_gll[r] = k;
+      s->rec_node[r] = gi + gj * s->nx_g;
+      s->rec_xy[2 * r] = s->xnode[gi];
+      s->rec_xy[2 * r + 1] = s->ynode[gj];
+    }
+  }
 
   /* CFL time step: smallest element size times half the smallest GLL gap, over the largest Vp */
   {

@@ -13,7 +13,8 @@
  * (fp64 is bit-identical to the reference), -cfl (0.5), -Lx -Ly (2000),
  * -x0 -y0 (-1000), -vp -vs -rho, -cells file (per-cell vp,vs,rho doubles),
  * -problem demo|explosion64|grf2048, -rec_file (x y per line), -block (steps per
- * device batch, default 100).
+ * device batch, default 100), -interp_receiver x,y (the interpolating receiver of
+ * RecordUV_interp, se2wave.c:2445-2581: its file and stdout line).
  *
  * The host set-up (libse2host) runs in FP64 on the CPU; the loop runs in
  * libse2gpu through its C-ABI.  There is no CPU fallback.
@@ -141,8 +142,9 @@ int main(int argc, char **argv)
 {
   int mx = 8, my, p = 2, nt_opt = -1, of = 5000, block = 100, r, s, ignore_rec, precision, dump_ic, ckpt_every = 0;
   const char *restart;
-  int sp_src_impl = -1;
-  double sp_sm_h = 0.0;
+  int sp_src_impl = -1, src_impl_raw = -1, ninterp = 0, nrec_all;
+  double sp_sm_h = 0.0, interp_xy[2] = {0.0, 0.0};
+  char fname_interp[512];
   double dvp = 0.0, dvs = 0.0, drho = 0.0;
   int perturb;
   double tmax = 0.4, dt_opt = 0.0, cfl = 0.5, Lx = 2000.0, Ly, x0 = -1000.0, y0, vp = 4746.3670317412243,
@@ -257,10 +259,18 @@ int main(int argc, char **argv)
       printf("  [source implementation]: processed from command line args\n");
       printf("  [source implementation]: %s\n", nm[impl]);
       sp_src_impl = (impl == 1) ? -1 : impl;   /* 1 = the nearest interior GLL point, the default path */
+      src_impl_raw = impl;
     }
     if (opt_real("-sm_h", &h)) sp_sm_h = h;
   }
   restart = opt_str("-restart", NULL);
+  {
+    const char *ir = opt_str("-interp_receiver", NULL);
+    if (ir) {
+      if (sscanf(ir, "%lf,%lf", &interp_xy[0], &interp_xy[1]) != 2) { fprintf(stderr, "-interp_receiver: expected x,y\n"); return 1; }
+      ninterp = 1;
+    }
+  }
   if (block < 1) block = 1;
   sp.nearest_internal_gll = opt_bool("-use_nearest_internal_gll", 1);
   sp.nsrc = nsrc; sp.src_xy = src_xy; sp.src_m = src_m; sp.stf_type = stf_type; sp.stf_par = stf_par;
@@ -268,6 +278,7 @@ int main(int argc, char **argv)
   if (!cell && perturb) { sp.perturb = 1; sp.dvp = dvp; sp.dvs = dvs; sp.drho = drho; }
   sp.src_impl = sp_src_impl;
   sp.sm_h = sp_sm_h;
+  sp.ninterp = ninterp; sp.interp_xy = interp_xy;
 
   if (!cell && perturb) {  /* se2wave.c:1228-1230 */
     printf("  [material]     Vp0 = %1.8e : delta = %+1.8e\n", vp, dvp);
@@ -314,6 +325,24 @@ int main(int argc, char **argv)
   /* receiver files: header of RecordUVA_MultipleStations_NearestGLL_MPI (2808-2882) */
   snprintf(fname, sizeof(fname), "closestqpsource-receiverCP-uva-%dx%d-p%d-rank%d.dat", mx, my, p, 0);
   snprintf(meta, sizeof(meta), "closestqpsource-receiverCP-uva-%dx%d-p%d.mpimeta", mx, my, p);
+  nrec_all = ignore_rec ? 0 : su->nrec;   /* the stations, then the interpolating receiver's element nodes */
+  {  /* RecordUV_interp's file name by source implementation (2458-2476) */
+    const char *kind[5] = {"defaultsource", "deltasource", "closestqpsource", "csplinesource", "p0source"};
+    snprintf(fname_interp, sizeof(fname_interp), "%s-receiver-%dx%d-p%d.dat", kind[src_impl_raw + 1], mx, my, p);
+  }
+  if (!ignore_rec && ninterp > 0 && !restart) {  /* its header (2478-2491) */
+    fp = fopen(fname_interp, "w");
+    if (!fp) { fprintf(stderr, "Failed to open file \"%s\"\n", fname_interp); return 1; }
+    fprintf(fp, "# SpecFECtx meta data\n");
+    fprintf(fp, "#   mx %d : my %d : basis order %d\n", mx, my, p);
+    fprintf(fp, "#   source implementation %d\n", src_impl_raw);
+    fprintf(fp, "# Receiver meta data\n");
+    fprintf(fp, "#   + receiver location: x,y %+1.8e %+1.8e\n", interp_xy[0], interp_xy[1]);
+    fprintf(fp, "#   + records displ/velo at requested receiver location through interpolating the FE solution\n");
+    fprintf(fp, "# Time series header\n");
+    fprintf(fp, "#   time ux uy vx vy\n");
+    fclose(fp);
+  }
   if (!ignore_rec && nrec > 0 && !restart) {
     fp = fopen(fname, "w");
     if (!fp) { fprintf(stderr, "Failed to open file \"%s\"\n", fname); return 1; }
@@ -369,16 +398,20 @@ int main(int argc, char **argv)
   {
     double *stf = (double*)malloc(sizeof(double) * (size_t)block * (nsrc > 0 ? nsrc : 1));
     double *times = (double*)malloc(sizeof(double) * (size_t)block);
-    double *rows = (double*)malloc(sizeof(double) * (size_t)(block + 1) * 7 * (nrec > 0 ? nrec : 1));
+    double *rows = (double*)malloc(sizeof(double) * (size_t)(block + 1) * 7 * (nrec_all > 0 ? nrec_all : 1));
+    double *irows = (double*)malloc(sizeof(double) * (size_t)(block + 1) * 7 * (ninterp > 0 ? ninterp : 1));
     double nrm[6];
     double *fu = (double*)malloc(sizeof(double) * 2 * (size_t)su->nnodes);
     double *fv = (double*)malloc(sizeof(double) * 2 * (size_t)su->nnodes);
     const char *vnames[2] = {"disp", "velo"};
     const double *vvecs[2] = {fu, fv};
+    if (!ignore_rec && ninterp > 0 && k == 0)   /* printed by RecordUV_interp's first call (2543) */
+      printf("# receiver location: x,y %+1.8e %+1.8e -- interpolated coordinate --> %+1.8e %+1.8e\n", interp_xy[0],
+             interp_xy[1], su->interp_xri[0], su->interp_xri[1]);
     for (; k < nsteps;) {
       long n = block - (k % block);
       long j;
-      int nr;
+      int nr = 0;
       if (n > of - (k % of)) n = of - (k % of);   /* end blocks on snapshot steps */
       if (ckpt_every > 0 && n > ckpt_every - (k % ckpt_every)) n = ckpt_every - (k % ckpt_every);
       if (k + n > nsteps) n = nsteps - k;
@@ -391,14 +424,23 @@ int main(int argc, char **argv)
         printf("  [displacement] max = %+1.4e : min = %+1.4e : l2 = %+1.4e \n", nrm[0], nrm[1], nrm[2]);
         printf("  [velocity]     max = %+1.4e : min = %+1.4e : l2 = %+1.4e \n", nrm[3], nrm[4], nrm[5]);
       }
+      if (nrec_all > 0) CHECK(nr = se2gpu_traces(h, rows, block + 1));
+      if (!ignore_rec && ninterp > 0) {  /* time ux uy vx vy (2571) */
+        if (se2_interp_rows(su, nr, rows, irows)) { fprintf(stderr, "%s\n", se2_host_last_error()); return 1; }
+        fp = fopen(fname_interp, "a");
+        if (!fp) { fprintf(stderr, "Failed to open file \"%s\"\n", fname_interp); return 1; }
+        for (j = 0; j < nr; j++)
+          fprintf(fp, "%1.4e %+1.8e %+1.8e %+1.8e %+1.8e\n", times[j], irows[7 * j], irows[7 * j + 1], irows[7 * j + 2],
+                  irows[7 * j + 3]);
+        fclose(fp);
+      }
       if (!ignore_rec && nrec > 0) {
-        CHECK(nr = se2gpu_traces(h, rows, block + 1));
         fp = fopen(fname, "a");
         if (!fp) { fprintf(stderr, "Failed to open file \"%s\"\n", fname); return 1; }
         for (j = 0; j < nr; j++) {
           fprintf(fp, "%1.4e", times[j]);
           for (r = 0; r < nrec; r++) {
-            const double *o = &rows[(size_t)j * 7 * nrec + 7 * r];
+            const double *o = &rows[(size_t)j * 7 * nrec_all + 7 * r];
             fprintf(fp, " %+1.8e %+1.8e %+1.8e %+1.8e %+1.8e %+1.8e", o[0], o[1], o[2], o[3], o[4], o[5]);
             fprintf(fp, " %+1.8e", o[6]);
           }
@@ -437,7 +479,7 @@ int main(int argc, char **argv)
     snprintf(fname_vts, sizeof(fname_vts), "step-%.4ld.vts", (time >= su->tmax) ? k : k + 1);
     CHECK(se2gpu_get_fields(h, fu, fv, NULL));
     if (se2_write_vts(su, fname_vts, 2, vnames, vvecs)) { fprintf(stderr, "%s\n", se2_host_last_error()); return 1; }
-    free(stf); free(times); free(rows); free(fu); free(fv);
+    free(stf); free(times); free(rows); free(irows); free(fu); free(fv);
   }
   se2gpu_destroy(h);
   se2_setup_destroy(su);

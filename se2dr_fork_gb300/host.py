@@ -27,7 +27,8 @@ class _CSpec(C.Structure):
                 ("nsrc", C.c_int), ("src_xy", _dp), ("src_m", _dp), ("stf_type", _ip), ("stf_par", _dp),
                 ("nrec", C.c_int), ("rec_xy", _dp),
                 ("perturb", C.c_int), ("dvp", C.c_double), ("dvs", C.c_double), ("drho", C.c_double),
-                ("src_impl", C.c_int), ("sm_h", C.c_double)]
+                ("src_impl", C.c_int), ("sm_h", C.c_double),
+                ("ninterp", C.c_int), ("interp_xy", _dp)]
 
 
 class _CSetup(C.Structure):
@@ -42,7 +43,9 @@ class _CSetup(C.Structure):
                 ("nsrc", C.c_int), ("src_elem", _ip), ("src_gll", _ip), ("src_vals", _dp),
                 ("stf_type", _ip), ("stf_par", _dp),
                 ("nrec", C.c_int), ("rec_xy", _dp), ("rec_node", _ip), ("rec_elem", _ip), ("rec_gll", _ip),
-                ("nsrc_phys", C.c_int), ("src_owner", _ip)]
+                ("nsrc_phys", C.c_int), ("src_owner", _ip),
+                ("nrec_sta", C.c_int), ("ninterp", C.c_int), ("interp_xy", _dp), ("interp_elem", _ip),
+                ("interp_N", _dp), ("interp_xri", _dp)]
 
 
 class CShotDraw(C.Structure):
@@ -73,6 +76,8 @@ def lib():
         L.se2_gaussian_random_field.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                                 C.c_ulonglong, _dp]
         L.se2_source_vector.argtypes = [C.POINTER(_CSetup), C.c_int, C.c_double, _dp, _dp, _dp]
+        L.se2_interp_receiver.argtypes = [C.POINTER(_CSetup), _dp, _ip, _dp, _dp]
+        L.se2_interp_rows.argtypes = [C.POINTER(_CSetup), C.c_long, _dp, _dp]
         L.se2_shot_draw_params.argtypes = [C.c_ulonglong, C.c_long, C.c_int, C.POINTER(CShotDraw)]
         L.se2_shot_materials.argtypes = [C.POINTER(CShotDraw), _dp, _dp, _dp]
         _lib = L
@@ -115,6 +120,10 @@ class _SpecHolder:
             cs.perturb = 1
             cs.dvp, cs.dvs, cs.drho = spec.perturb
         cs.src_impl, cs.sm_h = int(spec.src_impl), float(spec.sm_h)
+        ixy = np.array(spec.interp_receivers, dtype=np.float64).reshape(-1)
+        self.keep.append(ixy)
+        cs.ninterp = len(spec.interp_receivers)
+        cs.interp_xy = _p(ixy)
         self.cs = cs
 
 
@@ -161,6 +170,11 @@ class Setup:
         self.rec_gll = _arr(s.rec_gll, self.nrec, np.int32)
         self.nsrc_phys = s.nsrc_phys
         self.src_owner = _arr(s.src_owner, self.nsrc, np.int32)
+        # receiver list = nrec_sta stations, then npe element nodes per interpolating receiver
+        self.nrec_sta, self.ninterp = s.nrec_sta, s.ninterp
+        self.interp_elem = _arr(s.interp_elem, self.ninterp, np.int32)
+        self.interp_N = _arr(s.interp_N, self.ninterp * npe).reshape(self.ninterp, npe)
+        self.interp_xri = _arr(s.interp_xri, 2 * self.ninterp).reshape(self.ninterp, 2)
 
     def __del__(self):
         if getattr(self, "_ptr", None):
@@ -189,6 +203,27 @@ class Setup:
         if lib().se2_source_vector(self._ptr, int(impl), float(kernel_h), _p(xy), _p(m), _p(g)) != 0:
             raise ValueError(_err())
         return g
+
+    def interp_receiver(self, xy) -> Tuple[int, np.ndarray, np.ndarray]:
+        """(element, weights N[npe], interpolated coordinate) of a point (se2_interp_receiver)."""
+        xy = np.ascontiguousarray(xy, dtype=np.float64)
+        eid, N, xri = C.c_int(), np.zeros(self.npe), np.zeros(2)
+        if lib().se2_interp_receiver(self._ptr, _p(xy), C.byref(eid), _p(N), _p(xri)) != 0:
+            raise ValueError(_err())
+        return eid.value, N, xri
+
+    def interp_rows(self, rows: np.ndarray) -> np.ndarray:
+        """Receiver rows [nsteps][(1 +) 7*nrec] (with or without the time column) -> the
+        interpolating receivers' rows [nsteps][ninterp][7] (se2_interp_rows)."""
+        rows = np.asarray(rows, dtype=np.float64)
+        if rows.shape[1] == 1 + 7 * self.nrec:
+            rows = rows[:, 1:]
+        rows = np.ascontiguousarray(rows)
+        assert rows.shape[1] == 7 * self.nrec
+        out = np.zeros((rows.shape[0], self.ninterp, 7))
+        if lib().se2_interp_rows(self._ptr, rows.shape[0], _p(rows), _p(out)) != 0:
+            raise ValueError(_err())
+        return out
 
     def stf_block(self, time: float, n: int) -> Tuple[np.ndarray, np.ndarray, float]:
         """Times and STF values of the next n steps after `time`."""

@@ -72,6 +72,9 @@ class Spec:
     # 2 cubic-spline kernel of radius sm_h (<= 0: default), 3 P0 (se2wave.c:2202-2266, -source_impl)
     src_impl: int = -1
     sm_h: float = 0.0
+    # interpolating receivers (RecordUV_interp, se2wave.c:2445-2581): u, v (and a, curl v) at the
+    # exact points from the Lagrange interpolant of the containing element
+    interp_receivers: List[Tuple[float, float]] = field(default_factory=list)
 
     @property
     def ne(self) -> int:
@@ -122,6 +125,8 @@ class Spec:
             lines.append(f"src {float(s.x)!r} {float(s.y)!r} {m} {_STF_NAMES[s.stf]} {par}")
         for (x, y) in self.receivers:
             lines.append(f"rec {float(x)!r} {float(y)!r}")
+        for (x, y) in self.interp_receivers:   # the reference driver keeps one (RecordUV_interp's static state)
+            lines.append(f"irec {float(x)!r} {float(y)!r}")
         return "\n".join(lines) + "\n"
 
 

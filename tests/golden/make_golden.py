@@ -69,6 +69,8 @@ def spec_arrays(sp: S.Spec) -> dict:
         d.update(cell_vp=np.asarray(sp.cell_vp), cell_vs=np.asarray(sp.cell_vs), cell_rho=np.asarray(sp.cell_rho))
     if sp.perturb is not None:
         d.update(perturb=np.array(sp.perturb, dtype=np.float64))
+    if sp.interp_receivers:
+        d.update(interp_xy=np.array(sp.interp_receivers, dtype=np.float64).reshape(-1, 2))
     return {"spec_" + k: v for k, v in d.items()}
 
 
@@ -90,6 +92,24 @@ def perturbed():
         raise RuntimeError(r["stderr"])
     res = run_case(sp, fields=True)
     save("perturbed_p3", cell_lmr=r["cell_lmr"], **res, **spec_arrays(sp))
+
+
+def interp():
+    """Interpolating receiver RecordUV_interp (se2wave.c:2445-2581) on a heterogeneous mesh,
+    p = 3 and 4, one point inside an element and one on an element edge (xi = -1)."""
+    for p, xy in ((3, (137.3, -251.9)), (4, (-250.0, 311.7))):
+        rng = np.random.default_rng(40 + p)
+        mx, my = 9, 7
+        sp = S.demo(mx, my, p=p, tmax=1.0).replace(
+            nt=50, name=f"interp_p{p}", interp_receivers=[xy],
+            cell_vp=rng.uniform(5000, 7000, mx * my), cell_vs=rng.uniform(2800, 3500, mx * my),
+            cell_rho=rng.uniform(2000, 3000, mx * my))
+        r = O.ref_run(sp)
+        if r["returncode"] != 0:
+            raise RuntimeError(r["stderr"])
+        fname = f"defaultsource-receiver-{mx}x{my}-p{p}.dat"
+        save(f"interp_p{p}", interp=r["interp"], interp_xri_text=r["interp_xri_text"], traces=r["traces"],
+             u=r["u"], v=r["v"], dat_name=np.array(fname), dat_text=np.array(r[fname]), **spec_arrays(sp))
 
 
 def run_case(sp: S.Spec, fields: bool, extra=()):
@@ -130,6 +150,10 @@ def main():
         perturbed()
         source_vectors()
         return
+    if "--interp-only" in sys.argv:
+        O.build_ref()
+        interp()
+        return
     if "--cli-only" in sys.argv:
         O.build_ref()
         reference_main_outputs([], "cli_demo_default")
@@ -151,6 +175,7 @@ def main():
 
     perturbed()
     source_vectors()
+    interp()
 
     print("internal force AssembleLinearForm_ElastoDynamics2d on random displacements")
     for p, mx, my in [(1, 6, 5), (3, 6, 5), (4, 9, 10), (7, 3, 4)]:

@@ -26,6 +26,8 @@ def spec_of(d) -> S.Spec:
         sp = sp.replace(cell_vp=g("cell_vp"), cell_vs=g("cell_vs"), cell_rho=g("cell_rho"))
     if "spec_perturb" in d:
         sp = sp.replace(perturb=tuple(float(x) for x in g("perturb")))
+    if "spec_interp_xy" in d:
+        sp = sp.replace(interp_receivers=[tuple(float(v) for v in r) for r in g("interp_xy")])
     return sp
 
 

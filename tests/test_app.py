@@ -138,3 +138,28 @@ def test_app_checkpoint_restart_continues_bitwise(app, tmp_path, precision):
     for f in os.listdir(b):
         if f.endswith(".vts"):
             assert open(a / f, "rb").read() == open(b / f, "rb").read(), f
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("p", [3, 4])
+def test_app_interp_receiver_file_matches_reference(app, tmp_path, p):
+    """-interp_receiver x,y writes RecordUV_interp's file (se2wave.c:2445-2581) byte for byte
+    as the reference does (FP64), prints its interpolated-coordinate line, and leaves the
+    multi-station file unchanged in layout."""
+    g = load(f"interp_p{p}")
+    mx, my = int(g["spec_mx"]), int(g["spec_my"])
+    cells = np.concatenate([g["spec_cell_vp"], g["spec_cell_vs"], g["spec_cell_rho"]]).astype(np.float64)
+    cells.tofile(tmp_path / "cells.bin")
+    x, y = (float(v) for v in g["spec_interp_xy"][0])
+    args = ["-mx", str(mx), "-my", str(my), "-bdegree", str(p), "-tmax", repr(float(g["spec_tmax"])),
+            "-nt", str(int(g["spec_nt"])), "-cells", "cells.bin", "-interp_receiver", f"{x!r},{y!r}"]
+    r = subprocess.run([app, *args], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    with open(tmp_path / str(g["dat_name"])) as f:
+        assert f.read() == str(g["dat_text"])
+    line = [l for l in r.stdout.splitlines() if "interpolated coordinate" in l]
+    assert len(line) == 1
+    assert np.array_equal([float(t) for t in line[0].split("-->")[1].split()], g["interp_xri_text"])
+    sta = np.loadtxt(tmp_path / f"closestqpsource-receiverCP-uva-{mx}x{my}-p{p}-rank0.dat", comments="#")
+    assert sta.shape == (g["traces"].shape[0], 1 + 7 * 3)
+    np.testing.assert_allclose(sta[:, 1:], g["traces"][:, 1:], rtol=1e-8, atol=1e-30)

@@ -65,6 +65,29 @@ def test_fp64_perturbed_materials_bitwise_vs_reference():
     assert np.array_equal(u, d["u"]) and np.array_equal(v, d["v"]) and np.array_equal(a, d["a"])
 
 
+@pytest.mark.parametrize("p", [3, 4])
+@pytest.mark.parametrize("precision", ["fp64", "fp32_kahan"])
+def test_interp_receiver_vs_reference(p, precision):
+    """The interpolating receiver (RecordUV_interp, se2wave.c:2445-2581): the element's nodes
+    ride in the device receiver list and the host combines their rows.  FP64 is bit-identical
+    to the reference's recorded u, v at every step; FP32+Kahan within the FP32 trace
+    tolerance of the other receivers."""
+    d = load(f"interp_p{p}")
+    su = H.Setup(spec_of(d))
+    tr = G.Solver(su, precision).run()
+    ip = su.interp_rows(tr)
+    ref = d["interp"]
+    assert ip.shape == (ref.shape[0], 1, 7)
+    assert np.array_equal(tr[:, 0], ref[:, 0])
+    got = ip[:, 0, :4]
+    if precision == "fp64":
+        assert np.array_equal(got, ref[:, 1:])
+        assert np.array_equal(tr[:, :1 + 7 * su.nrec_sta], d["traces"])
+    else:
+        for c, tol in enumerate(FP32_COMPONENT_TOL[:4]):
+            assert rel_l2(got[:, c], ref[:, 1 + c]) <= tol, (c, rel_l2(got[:, c], ref[:, 1 + c]))
+
+
 def test_fp64_explosion64_full_run_bitwise_vs_reference():
     d = load("explosion64")
     sol = G.Solver(H.Setup(spec_of(d)), "fp64")

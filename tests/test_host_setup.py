@@ -168,3 +168,53 @@ def test_source_entries_reassemble_the_vector(impl):
     assert np.array_equal(acc, g)
     times, stf, _ = su.stf_block(0.0, 7)
     assert stf.shape == (7, su.nsrc) and np.all(stf == stf[:, :1])
+
+
+@pytest.mark.parametrize("p", [3, 4])
+def test_interp_receiver_vs_reference(p):
+    """RecordUV_interp (se2wave.c:2445-2581): element, weights and interpolated coordinate of
+    the host set-up; the weighted sum over the element's nodes of the reference's final
+    fields reproduces the reference's last recorded row bit for bit."""
+    d = load(f"interp_p{p}")
+    sp = spec_of(d)
+    su = H.Setup(sp)
+    assert su.ninterp == 1 and su.nrec_sta == len(sp.receivers) and su.nrec == su.nrec_sta + su.npe
+    # the coordinate the reference prints (%+1.8e)
+    np.testing.assert_allclose(su.interp_xri[0], d["interp_xri_text"], rtol=1e-8, atol=1e-6)
+    assert abs(su.interp_N[0].sum() - 1.0) < 1e-12
+    # the appended receiver entries are the element's nodes in ascending local order
+    e = int(su.interp_elem[0])
+    base = su.nrec_sta
+    for k in range(su.npe):
+        node = (e % su.mx * su.p + k % su.n1) + (e // su.mx * su.p + k // su.n1) * su.nx_g
+        assert su.rec_elem[base + k] == e and su.rec_gll[base + k] == k and su.rec_node[base + k] == node
+    vals = []
+    for arr in (d["u"], d["v"]):
+        for c in range(2):
+            acc = 0.0
+            for k in range(su.npe):
+                acc += float(su.interp_N[0, k]) * float(arr[2 * su.rec_node[base + k] + c])
+            vals.append(acc)
+    assert same(np.array(vals), d["interp"][-1, 1:])
+    # se2_interp_rows combines receiver rows in the same order
+    rng = np.random.default_rng(p)
+    rows = rng.standard_normal((4, 7 * su.nrec))
+    out = su.interp_rows(rows)
+    for j in range(4):
+        for c in range(7):
+            acc = 0.0
+            for k in range(su.npe):
+                acc += float(su.interp_N[0, k]) * float(rows[j, 7 * (base + k) + c])
+            assert out[j, 0, c] == acc
+
+
+def test_interp_receiver_rejects_points_outside_the_mesh():
+    sp = S.demo(9, 7, p=3, tmax=1.0)
+    su = H.Setup(sp)
+    for xy in [(1000.0, 0.0), (0.0, 1000.0), (-1000.1, 0.0), (0.0, -2000.0)]:
+        with pytest.raises(ValueError, match="interpolating receiver"):
+            su.interp_receiver(xy)
+        with pytest.raises(ValueError, match="interpolating receiver"):
+            H.Setup(sp.replace(interp_receivers=[xy]))
+    e, N, xri = su.interp_receiver((-1000.0, -1000.0))     # the domain corner: element 0, xi = eta = -1
+    assert e == 0 and N[0] == 1.0 and np.all(N[1:] == 0.0)
