@@ -103,6 +103,11 @@ __host__ __device__ constexpr int round_up(int x, int m) { return (x + m - 1) / 
 template <int P, int TE>
 struct Geo {
   static constexpr int N1 = P + 1, NPE = N1 * N1;
+  // element stride of the exchange buffers: (p+1)^2 node values plus a pad that spreads
+  // the elements a warp touches over the 32 banks (with (p+1)^2 = 16 at p = 3 every
+  // element would start on bank 0; pads chosen with a wavefront model of the kernel's
+  // accesses)
+  static constexpr int XS = NPE + (P == 1 ? 2 : P == 3 ? 3 : P == 6 ? 6 : P == 7 ? 7 : P == 8 ? 8 : 0);
   static constexpr int NEX = TE + 1, NE = NEX * NEX;      // elements incl. halo
   static constexpr int ITEMS = NE * N1;                   // (element, line) work items
   // region box (u, cu): the x start is rounded down to an even node so the copy
@@ -125,7 +130,7 @@ struct Layout {
   static constexpr size_t REG = al128(sizeof(float2) * G::BXW * G::BXH);
   static constexpr size_t OWN = al128(sizeof(float2) * G::OBW * G::OBH);
   static constexpr size_t STAGE = (REG + OWN) * (KAHAN ? 2 : 1);
-  static constexpr size_t XCH = al128(sizeof(float2) * G::NE * G::NPE);   // exchange buffer
+  static constexpr size_t XCH = al128(sizeof(float2) * G::NE * G::XS);    // exchange buffer
   static constexpr size_t MISC = 64;
   static constexpr size_t TOTAL = 2 * STAGE + 2 * XCH + MISC;
   // the batched kernel keeps the shot parameters of the current and the next tile after the barriers
@@ -213,7 +218,7 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
 {
   typedef Geo<P, TE> G;
   typedef Layout<P, TE, KAHAN> L;
-  constexpr int N1 = G::N1, NPE = G::NPE, NEX = G::NEX, BXW = G::BXW, OBW = G::OBW;
+  constexpr int N1 = G::N1, NPE = G::NPE, NEX = G::NEX, BXW = G::BXW, OBW = G::OBW, XS = G::XS;
   const float *D = c_D[P - 1];
   const float *W = c_w[P - 1];
   const TileBox b = tile_box<P, TE>(prm, tx, ty);
@@ -308,7 +313,7 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
         float sx = 0.f, sy = 0.f;
 #pragma unroll
         for (int k = 1; k < N1; k++) { sx = fmaf(D[q * N1 + k], d[k].x, sx); sy = fmaf(D[q * N1 + k], d[k].y, sy); }
-        X1[el * NPE + j + q * N1] = make_float2(sx, sy);   // d/deta at (j, q)
+        X1[el * XS + j + q * N1] = make_float2(sx, sy);   // d/deta at (j, q)
       }
     }
   }
@@ -321,13 +326,13 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
     float2 Fxi[N1];
 #pragma unroll
     for (int q = 0; q < N1; q++) {
-      const float2 ge = X1[el * NPE + q + j * N1];   // d/deta at (q, j)
+      const float2 ge = X1[el * XS + q + j * N1];   // d/deta at (q, j)
       const float e0 = ix * gxi[q].x, e1 = iy * ge.y, e2 = fmaf(ix, gxi[q].y, iy * ge.x);
       const float nf = nfj * W[q];                   // -detJ w_q w_j
       const float fx_ = ix * nf, fy_ = iy * nf;
       const float sxx = fmaf(c11, e0, lam * e1), syy = fmaf(lam, e0, c11 * e1), sxy = mu * e2;
       Fxi[q] = make_float2(fx_ * sxx, fx_ * sxy);
-      X2[el * NPE + q + j * N1] = make_float2(fy_ * sxy, fy_ * syy);
+      X2[el * XS + q + j * N1] = make_float2(fy_ * sxy, fy_ * syy);
     }
     // xi part of the divergence for the row's nodes, to X1 (this thread alone read row j of X1)
 #pragma unroll
@@ -335,7 +340,7 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
       float rx = 0.f, ry = 0.f;
 #pragma unroll
       for (int q = 0; q < N1; q++) { rx = fmaf(D[q * N1 + a], Fxi[q].x, rx); ry = fmaf(D[q * N1 + a], Fxi[q].y, ry); }
-      X1[el * NPE + a + j * N1] = make_float2(rx, ry);
+      X1[el * XS + a + j * N1] = make_float2(rx, ry);
     }
   }
   __syncthreads();
@@ -344,14 +349,14 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
   if (active) {
     float2 fc[N1];
 #pragma unroll
-    for (int q = 0; q < N1; q++) fc[q] = X2[el * NPE + j + q * N1];
+    for (int q = 0; q < N1; q++) fc[q] = X2[el * XS + j + q * N1];
 #pragma unroll
     for (int bq = 0; bq < N1; bq++) {
-      const float2 r = X1[el * NPE + j + bq * N1];
+      const float2 r = X1[el * XS + j + bq * N1];
       float cx = r.x, cy = r.y;
 #pragma unroll
       for (int q = 0; q < N1; q++) { cx = fmaf(D[q * N1 + bq], fc[q].x, cx); cy = fmaf(D[q * N1 + bq], fc[q].y, cy); }
-      X1[el * NPE + j + bq * N1] = make_float2(cx, cy);
+      X1[el * XS + j + bq * N1] = make_float2(cx, cy);
     }
   }
   __syncthreads();
@@ -376,10 +381,10 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
         const int ex = lx / P, ey = ly / P, ix = lx - ex * P, iy = ly - ey * P;
         const bool in_x = X < NXP, in_y = Y < NYP;
         const bool lft = (ix == 0) && (X > 0), bot = (iy == 0) && (Y > 0);
-        const int own = (ey * NEX + ex) * NPE + ix + iy * N1;
-        if (bot && lft) { const float2 fe = X1[own - NEX * NPE - NPE + P + P * N1]; fx += fe.x; fy += fe.y; }
-        if (bot && in_x) { const float2 fe = X1[own - NEX * NPE + P * N1]; fx += fe.x; fy += fe.y; }
-        if (lft && in_y) { const float2 fe = X1[own - NPE + P]; fx += fe.x; fy += fe.y; }
+        const int own = (ey * NEX + ex) * XS + ix + iy * N1;
+        if (bot && lft) { const float2 fe = X1[own - NEX * XS - XS + P + P * N1]; fx += fe.x; fy += fe.y; }
+        if (bot && in_x) { const float2 fe = X1[own - NEX * XS + P * N1]; fx += fe.x; fy += fe.y; }
+        if (lft && in_y) { const float2 fe = X1[own - XS + P]; fx += fe.x; fy += fe.y; }
         if (in_x && in_y) { const float2 fe = X1[own]; fx += fe.x; fy += fe.y; }
       }
       for (int q = s0; q < s1; q++) {
@@ -440,10 +445,10 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
       const int ex = lx / P, ey = ly / P, ix = lx - ex * P, iy = ly - ey * P;
       const bool in_x = X < NXP, in_y = Y < NYP;
       const bool lft = (ix == 0) && (X > 0), bot = (iy == 0) && (Y > 0);
-      const int own = (ey * NEX + ex) * NPE + ix + iy * N1;
-      if (bot && lft) { const float2 fe = X1[own - NEX * NPE - NPE + P + P * N1]; f[h][0] += fe.x; f[h][1] += fe.y; }
-      if (bot && in_x) { const float2 fe = X1[own - NEX * NPE + P * N1]; f[h][0] += fe.x; f[h][1] += fe.y; }
-      if (lft && in_y) { const float2 fe = X1[own - NPE + P]; f[h][0] += fe.x; f[h][1] += fe.y; }
+      const int own = (ey * NEX + ex) * XS + ix + iy * N1;
+      if (bot && lft) { const float2 fe = X1[own - NEX * XS - XS + P + P * N1]; f[h][0] += fe.x; f[h][1] += fe.y; }
+      if (bot && in_x) { const float2 fe = X1[own - NEX * XS + P * N1]; f[h][0] += fe.x; f[h][1] += fe.y; }
+      if (lft && in_y) { const float2 fe = X1[own - XS + P]; f[h][0] += fe.x; f[h][1] += fe.y; }
       if (in_x && in_y) { const float2 fe = X1[own]; f[h][0] += fe.x; f[h][1] += fe.y; }
       for (int q = s0; q < s1; q++) {
         const int sidx = prm.tile_src_idx[q], se = prm.src_elem[sidx], sx = se % prm.mx, sy = se / prm.mx;
