@@ -139,6 +139,14 @@ struct Layout {
       (uint32_t)((KAHAN ? 2 : 1) * (sizeof(float2) * G::BXW * G::BXH + sizeof(float2) * G::OBW * G::OBH));
 };
 
+// CTAs per SM the register budget is sized for: as many as the shared memory allows (up
+// to 3; 228 KB per SM, 1 KB reserved per CTA).  Three CTAs cap small tiles at 65536 /
+// (3 NT) registers, which they fit without spilling, and hide more shared-memory latency.
+__host__ __device__ constexpr int min_blocks(size_t smem)
+{
+  return (3 * (smem + 1024) <= 233472) ? 3 : (2 * (smem + 1024) <= 233472) ? 2 : 1;
+}
+
 struct TileBox {
   int ex0, ex1, ey0, ey1, EX0, EY0, NEXa, NEYa, X0, Y0, OW, OH, RXa, RYa, OXa;
 };
@@ -519,7 +527,7 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
 }
 
 template <int P, int TE, int NT, bool KAHAN>
-__global__ void __launch_bounds__(NT, ((2 * (Layout<P, TE, KAHAN>::TOTAL + 1024) <= 233472) ? 2 : 1))
+__global__ void __launch_bounds__(NT, min_blocks(Layout<P, TE, KAHAN>::TOTAL))
 persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ CUtensorMap tm_cu,
              const __grid_constant__ CUtensorMap tm_w, const __grid_constant__ CUtensorMap tm_cw,
              const Params prm)
@@ -611,7 +619,7 @@ __device__ __forceinline__ void copy_params_async(Params *dst, const Params *src
 }
 
 template <int P, int TE, int NT, bool KAHAN>
-__global__ void __launch_bounds__(NT, ((2 * (Layout<P, TE, KAHAN>::BATCH_TOTAL + 1024) <= 233472) ? 2 : 1))
+__global__ void __launch_bounds__(NT, min_blocks(Layout<P, TE, KAHAN>::BATCH_TOTAL))
 persist_batch(const BatchArgs ba)
 {
   typedef Geo<P, TE> G;
