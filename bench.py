@@ -204,7 +204,7 @@ def run_ours(args, rank, world):
     def tmax(x):
         return replica_seconds(x, dist, "cuda")
 
-    spec = S.grf2048(args.mx, args.mx, p=4, nt=args.steps + args.warmup + 10)
+    spec = S.grf2048(args.mx, args.mx, p=args.degree, nt=args.steps + args.warmup + 10)
     setup = H.Setup(spec)
     nnodes, ne = setup.nnodes, setup.mx * setup.my
     dof = 2 * nnodes
@@ -239,7 +239,8 @@ def run_ours(args, rank, world):
                                       "achieved": achieved, "peak": hbm, "unit": "GB/s",
                                       "frac": achieved / hbm,
                                       "traffic": (MEASURED_TRAFFIC_PER_NODE[prec] * nnodes
-                                                  if prec in MEASURED_TRAFFIC_PER_NODE and args.mx == 2048 else None),
+                                                  if prec in MEASURED_TRAFFIC_PER_NODE and args.mx == 2048
+                                                  and args.degree == 4 else None),
                                       "traffic_note": "ncu DRAM bytes per node at 1024^2 x nodes (bytes per launch)",
                                       "alg_bytes_per_node": b, "peak_kind": peak_kind}}
 
@@ -281,7 +282,7 @@ def run_ours(args, rank, world):
     line = {"metric": METRIC, "value": head["value"], "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32" if prec != "fp64" else "f64", "data": "synthetic",
-            "config": {"workload": f"grf2048: {args.mx}x{args.mx} elements, degree 4, 20 km square, "
+            "config": {"workload": f"grf2048: {args.mx}x{args.mx} elements, degree {args.degree}, 20 km square, "
                                    f"Gaussian-random-field Vp (mean 5000, 10% std, corr 8 cells), Vp/Vs 1.73, "
                                    f"rho 2700, explosive Ricker f0 8 Hz, 64 receivers",
                        "precision": prec, "nodes": nnodes, "dof": dof, "parallelism": f"replicas x{world}",
@@ -554,6 +555,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["fp32_kahan", "fp32", "fp64"], default="fp32_kahan")
     ap.add_argument("--mx", type=int, default=2048, help="elements per side (default: the 2048^2 workload)")
+    ap.add_argument("--degree", type=int, default=4, help="polynomial degree of the single-solve run (default 4)")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-rows", type=int, default=32)
