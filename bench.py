@@ -228,7 +228,7 @@ def run_ours(args, rank, world):
         with ClockSampler(local) as clk:
             secs, launches = time_steps(sol, k, args.warmup, stream, torch)
         secs = tmax(secs)
-        tile = sol.tile_configs()[sol.tile_config] if prec != "fp64" else None
+        tile = sol.tile_config_info(sol.tile_config) if prec != "fp64" else None
         sol.close()
         per = secs / k
         b = alg_bytes_per_node(prec, ne, nnodes)
@@ -328,7 +328,7 @@ def run_sweep(args):
                 autotune.apply(sol, prec)
             sol.set_stream(stream.cuda_stream)
             secs, launches = time_steps(sol, k, args.warmup, stream, torch)
-            tile = sol.tile_configs()[sol.tile_config] if prec != "fp64" else None
+            tile = sol.tile_config_info(sol.tile_config) if prec != "fp64" else None
             sol.close()
             per = secs / k
             b = alg_bytes_per_node(prec, setup.mx * setup.my, setup.nnodes)

@@ -119,6 +119,11 @@ int se2gpu_device_fields(const se2gpu_solver *h, void **u, void **v, void **a);
    returns how many exist.  se2gpu_set_tile_config selects one (default 0). */
 int se2gpu_tile_configs(const se2gpu_solver *h, int *edge, int *threads, int max_configs);
 int se2gpu_set_tile_config(se2gpu_solver *h, int config);
+/* One configuration in full (no counterpart in the reference): info = {elements per
+   tile edge, threads per CTA, owned-box buffers (2: the next tile's w arrives a tile
+   ahead; 1: during the tile's element phases; 0: FP64), resident CTAs per SM on the
+   current device (0: FP64)}.  Two configurations may share edge and threads. */
+int se2gpu_tile_config_info(const se2gpu_solver *h, int config, int info[4]);
 
 /* ---- Checkpoint / resume (no counterpart in the reference, which restarts from
    t = 0).  The checkpoint holds the handle's whole evolving state: the fields

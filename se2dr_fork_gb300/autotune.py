@@ -70,11 +70,12 @@ def tune(setup, precision: str = "fp32_kahan", steps: int = 10, write: bool = Tr
     """Measure every configuration on `setup`; return {config, edge, threads, seconds, all}."""
     sol = Solver(setup, precision, trace_capacity=2 * steps + 8)
     configs = sol.tile_configs()
+    infos = [sol.tile_config_info(c) for c in range(len(configs))]
     times = [time_config(sol, c, steps) for c in range(len(configs))]
     sol.close()
     best = min(range(len(times)), key=lambda c: times[c])
     res = {"config": best, "edge": configs[best][0], "threads": configs[best][1], "seconds": times[best],
-           "all": [{"edge": e, "threads": t, "seconds": s} for (e, t), s in zip(configs, times)]}
+           "all": [dict(info, seconds=s) for info, s in zip(infos, times)]}
     if write:
         db = load()
         db[key(setup, precision)] = res

@@ -696,6 +696,26 @@ extern "C" int se2gpu_tile_configs(const se2gpu_solver *h, int *edge, int *threa
   return n;
 }
 
+extern "C" int se2gpu_tile_config_info(const se2gpu_solver *h, int config, int info[4])
+{
+  if (!h || !info) return SE2GPU_ERR_ARG;
+  if (is_f64(h)) {
+    if (config != 0) return SE2GPU_ERR_ARG;
+    info[0] = se2::tile_edge(h->p); info[1] = 256; info[2] = 0; info[3] = 0;
+    return 0;
+  }
+  se2p::TileShape ts;
+  if (config < 0 || se2p::config_shape(h->p, config, is_kahan(h), &ts)) return SE2GPU_ERR_ARG;
+  info[0] = ts.tex; info[1] = ts.nt; info[2] = ts.owned_buffers;
+  // the occupancy query needs the kernel's dynamic shared-memory limit raised first
+  if (cudaSetDevice(h->device) != cudaSuccess || se2p::prepare(h->p, config, is_kahan(h)) != cudaSuccess) {
+    cudaGetLastError();
+    return SE2GPU_ERR_CUDA;
+  }
+  info[3] = se2p::occupancy(h->p, config, is_kahan(h), false);
+  return 0;
+}
+
 extern "C" int se2gpu_set_tile_config(se2gpu_solver *h, int config)
 {
   if (!h) return SE2GPU_ERR_ARG;

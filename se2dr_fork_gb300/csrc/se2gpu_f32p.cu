@@ -21,40 +21,45 @@ cudaError_t set_tables(int p, const double *D, const double *w1d)
 
 // ---- one configuration = (degree, elements per tile edge, threads) ----------
 struct Entry {
-  int p, te, nt;
+  int p, te, nt, nob;
   size_t smem[2];                 // [kahan]
   size_t bsmem[2];                // batched kernel [kahan]
   const void *fn[2];              // persist_step<...> [kahan]
   const void *bfn[2];             // persist_batch<...> [kahan]
 };
 
-template <int P, int TE, int NT, bool K>
-static constexpr int min_blocks() { return (2 * (Layout<P, TE, K>::TOTAL + 1024) <= 233472) ? 2 : 1; }
-
-template <int P, int TE, int NT>
+template <int P, int TE, int NT, int NOB = owned_buffers(P), int MINB = 0>
 static Entry entry()
 {
+  constexpr int M0 = MINB ? MINB : min_blocks(Layout<P, TE, false, NOB>::TOTAL);
+  constexpr int M1 = MINB ? MINB : min_blocks(Layout<P, TE, true, NOB>::TOTAL);
+  constexpr int B0 = MINB ? MINB : min_blocks(Layout<P, TE, false, NOB>::BATCH_TOTAL);
+  constexpr int B1 = MINB ? MINB : min_blocks(Layout<P, TE, true, NOB>::BATCH_TOTAL);
   Entry e;
-  e.p = P; e.te = TE; e.nt = NT;
-  e.smem[0] = Layout<P, TE, false>::TOTAL;
-  e.smem[1] = Layout<P, TE, true>::TOTAL;
-  e.bsmem[0] = Layout<P, TE, false>::BATCH_TOTAL;
-  e.bsmem[1] = Layout<P, TE, true>::BATCH_TOTAL;
-  e.fn[0] = (const void *)persist_step<P, TE, NT, false>;
-  e.fn[1] = (const void *)persist_step<P, TE, NT, true>;
-  e.bfn[0] = (const void *)persist_batch<P, TE, NT, false>;
-  e.bfn[1] = (const void *)persist_batch<P, TE, NT, true>;
+  e.p = P; e.te = TE; e.nt = NT; e.nob = NOB;
+  e.smem[0] = Layout<P, TE, false, NOB>::TOTAL;
+  e.smem[1] = Layout<P, TE, true, NOB>::TOTAL;
+  e.bsmem[0] = Layout<P, TE, false, NOB>::BATCH_TOTAL;
+  e.bsmem[1] = Layout<P, TE, true, NOB>::BATCH_TOTAL;
+  e.fn[0] = (const void *)persist_step<P, TE, NT, false, NOB, M0>;
+  e.fn[1] = (const void *)persist_step<P, TE, NT, true, NOB, M1>;
+  e.bfn[0] = (const void *)persist_batch<P, TE, NT, false, NOB, B0>;
+  e.bfn[1] = (const void *)persist_batch<P, TE, NT, true, NOB, B1>;
   return e;
 }
 
-// every (element, line) item of a tile gets its own thread: NT >= (TE+1)^2 (P+1)
+// every (element, line) item of a tile gets its own thread: NT >= (TE+1)^2 (P+1).
+// entry<P, TE, NT, owned buffers, CTAs per SM the registers are sized for (0: as many
+// as the shared memory allows, up to 3)>
 static const Entry *table(int *n)
 {
   static Entry t[] = {
       entry<1, 15, 512>(), entry<1, 11, 288>(),
       entry<2, 10, 384>(), entry<2, 8, 256>(),
       entry<3, 8, 352>(),  entry<3, 7, 256>(),
-      entry<4, 7, 320>(),  entry<4, 6, 256>(), entry<4, 8, 416>(),
+      // degree 4: 7x7 with one owned buffer kept at 2 CTAs per SM (92 registers) is the
+      // fastest; sized for 3 CTAs it is capped at 64 registers and runs slower
+      entry<4, 7, 320, 1, 2>(), entry<4, 7, 320, 2>(), entry<4, 6, 256, 2>(), entry<4, 8, 416>(),
       entry<5, 6, 320>(),  entry<5, 5, 224>(),
       entry<6, 5, 256>(),  entry<6, 4, 192>(),
       entry<7, 5, 288>(),  entry<7, 4, 224>(),
@@ -94,6 +99,7 @@ int config_shape(int p, int config, bool kahan, TileShape *s)
   s->region_h = (e->te + 1) * p + 1;
   s->own_w = round_up(e->te * p + 2, 2);
   s->own_h = e->te * p + 1;
+  s->owned_buffers = e->nob;
   s->smem = e->smem[kahan ? 1 : 0];
   return 0;
 }

@@ -124,19 +124,30 @@ struct Geo {
 
 __host__ __device__ constexpr size_t al128(size_t x) { return (x + 127) & ~size_t(127); }
 
-template <int P, int TE, bool KAHAN>
+// owned-box buffers per degree (the default of the tile configurations): 2 up to degree
+// 3 (the next tile's w, cw arrive with its region, a whole tile ahead), 1 above (the
+// current tile's arrive during its element phases; the smaller footprint is faster
+// there, and at degree 8 it fits 2 CTAs per SM instead of 1)
+__host__ __device__ constexpr int owned_buffers(int p) { return p <= 3 ? 2 : 1; }
+
+template <int P, int TE, bool KAHAN, int NOB = owned_buffers(P)>
 struct Layout {
   typedef Geo<P, TE> G;
   static constexpr size_t REG = al128(sizeof(float2) * G::BXW * G::BXH);
   static constexpr size_t OWN = al128(sizeof(float2) * G::OBW * G::OBH);
-  static constexpr size_t STAGE = (REG + OWN) * (KAHAN ? 2 : 1);
+  // the region boxes (u and cu) are double-buffered: the next tile's arrive while this
+  // tile is computed.  The owned boxes (w and cw) are read only by the node phase:
+  // NOB = 2 buffers hold this tile's and the next's, NOB = 1 this tile's only.
+  static constexpr size_t STAGE = REG * (KAHAN ? 2 : 1);
+  static constexpr size_t OWNB = OWN * (KAHAN ? 2 : 1);
   static constexpr size_t XCH = al128(sizeof(float2) * G::NE * G::XS);    // exchange buffer
   static constexpr size_t MISC = 64;
-  static constexpr size_t TOTAL = 2 * STAGE + 2 * XCH + MISC;
-  // the batched kernel keeps the shot parameters of the current and the next tile after the barriers
-  static constexpr size_t BATCH_TOTAL = TOTAL + 2 * al128(sizeof(Params));
-  static constexpr uint32_t TX_BYTES =
-      (uint32_t)((KAHAN ? 2 : 1) * (sizeof(float2) * G::BXW * G::BXH + sizeof(float2) * G::OBW * G::OBH));
+  static constexpr size_t TOTAL = 2 * STAGE + NOB * OWNB + 2 * XCH + MISC;
+  // the batched kernel keeps the shot parameters of the current and the next tile right
+  // after the barriers (MISC): two 16-byte aligned slots
+  static constexpr size_t BATCH_TOTAL = TOTAL + al128(2 * sizeof(Params));
+  static constexpr uint32_t TX_REGION = (uint32_t)((KAHAN ? 2 : 1) * sizeof(float2) * G::BXW * G::BXH);
+  static constexpr uint32_t TX_OWNED = (uint32_t)((KAHAN ? 2 : 1) * sizeof(float2) * G::OBW * G::OBH);
 };
 
 // CTAs per SM the register budget is sized for: as many as the shared memory allows (up
@@ -168,11 +179,25 @@ __device__ __forceinline__ TileBox tile_box(const Params &prm, int tx, int ty)
   return b;
 }
 
-// issue the copies of tile (tx, ty) into a stage.  The box origins depend only on the
-// tile coordinates (the same formulas as tile_box); boxes reaching past the mesh
-// read the tensor maps' zero fill.
+// TMA copies of tile (tx, ty).  The box origins depend only on the tile coordinates
+// (the same formulas as tile_box); boxes reaching past the mesh read the tensor maps'
+// zero fill.  issue_region: the u (and cu) region box into a stage; issue_owned: the w
+// (and cw) owned box into the owned buffer.
 template <int P, int TE, bool KAHAN>
-__device__ __forceinline__ void issue_tile(int tx, int ty, unsigned char *stage, uint32_t bar,
+__device__ __forceinline__ void issue_region(int tx, int ty, unsigned char *stage, uint32_t bar,
+                                             const CUtensorMap *tm_u, const CUtensorMap *tm_cu)
+{
+  typedef Layout<P, TE, KAHAN> L;
+  const int ex0 = tx * TE, ey0 = ty * TE;
+  const int RXa = (max(ex0 - 1, 0) * P) & ~1, RYa = max(ey0 - 1, 0) * P;
+  mbar_expect_tx(bar, L::TX_REGION);
+  tma_load_2d(smem_u32(stage), tm_u, RXa, RYa, bar);
+  if (KAHAN) tma_load_2d(smem_u32(stage + L::REG), tm_cu, RXa, RYa, bar);
+}
+
+// the region and owned boxes of one tile on one barrier (two owned buffers)
+template <int P, int TE, bool KAHAN>
+__device__ __forceinline__ void issue_both(int tx, int ty, unsigned char *stage, unsigned char *ob, uint32_t bar,
                                            const CUtensorMap *tm_u, const CUtensorMap *tm_cu,
                                            const CUtensorMap *tm_w, const CUtensorMap *tm_cw)
 {
@@ -180,12 +205,22 @@ __device__ __forceinline__ void issue_tile(int tx, int ty, unsigned char *stage,
   const int ex0 = tx * TE, ey0 = ty * TE;
   const int RXa = (max(ex0 - 1, 0) * P) & ~1, RYa = max(ey0 - 1, 0) * P;
   const int OXa = (ex0 * P) & ~1, Y0 = ey0 * P;
-  mbar_expect_tx(bar, L::TX_BYTES);
-  size_t o = 0;
-  tma_load_2d(smem_u32(stage + o), tm_u, RXa, RYa, bar); o += L::REG;
-  if (KAHAN) { tma_load_2d(smem_u32(stage + o), tm_cu, RXa, RYa, bar); o += L::REG; }
-  tma_load_2d(smem_u32(stage + o), tm_w, OXa, Y0, bar); o += L::OWN;
-  if (KAHAN) { tma_load_2d(smem_u32(stage + o), tm_cw, OXa, Y0, bar); }
+  mbar_expect_tx(bar, L::TX_REGION + L::TX_OWNED);
+  tma_load_2d(smem_u32(stage), tm_u, RXa, RYa, bar);
+  if (KAHAN) tma_load_2d(smem_u32(stage + L::REG), tm_cu, RXa, RYa, bar);
+  tma_load_2d(smem_u32(ob), tm_w, OXa, Y0, bar);
+  if (KAHAN) tma_load_2d(smem_u32(ob + L::OWN), tm_cw, OXa, Y0, bar);
+}
+
+template <int P, int TE, bool KAHAN>
+__device__ __forceinline__ void issue_owned(int tx, int ty, unsigned char *ob, uint32_t bar,
+                                            const CUtensorMap *tm_w, const CUtensorMap *tm_cw)
+{
+  typedef Layout<P, TE, KAHAN> L;
+  const int OXa = (tx * TE * P) & ~1, Y0 = ty * TE * P;
+  mbar_expect_tx(bar, L::TX_OWNED);
+  tma_load_2d(smem_u32(ob), tm_w, OXa, Y0, bar);
+  if (KAHAN) tma_load_2d(smem_u32(ob + L::OWN), tm_cw, OXa, Y0, bar);
 }
 
 __device__ __forceinline__ void kahan_add(float &s, float &c, float inc)
@@ -219,10 +254,10 @@ __device__ void sample_rows(const Params &prm, const float *rbuf_in, double *tra
 
 // one tile: prefetch of global values, wait for the tile's copies, the three
 // element phases and the node phase.  Returns false when the bounded wait expired.
-template <int P, int TE, int NT, bool KAHAN>
+template <int P, int TE, int NT, bool KAHAN, bool OWAIT>
 __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, const unsigned char *st, uint32_t bar,
-                                          uint32_t parity, float2 *X1, float2 *X2, int item, int el, int j, int ecx,
-                                          int ecy, float wj)
+                                          uint32_t parity, const unsigned char *ob, uint32_t bar_o, uint32_t par_o,
+                                          float2 *X1, float2 *X2, int item, int el, int j, int ecx, int ecy, float wj)
 {
   typedef Geo<P, TE> G;
   typedef Layout<P, TE, KAHAN> L;
@@ -275,8 +310,8 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
   if (__syncthreads_or(!ok)) return false;
   const float2 *rU = reinterpret_cast<const float2 *>(st);
   const float2 *rCU = reinterpret_cast<const float2 *>(st + L::REG);
-  const float2 *oW = reinterpret_cast<const float2 *>(st + (KAHAN ? 2 : 1) * L::REG);
-  const float2 *oCW = reinterpret_cast<const float2 *>(st + (KAHAN ? 2 : 1) * L::REG + L::OWN);
+  const float2 *oW = reinterpret_cast<const float2 *>(ob);
+  const float2 *oCW = reinterpret_cast<const float2 *>(ob + L::OWN);
 
   // ---- 1. derivatives along row j (registers) and column j (to X1) -----
   float2 gxi[N1];
@@ -367,7 +402,13 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
       X1[el * XS + j + bq * N1] = make_float2(cx, cy);
     }
   }
-  __syncthreads();
+  if (OWAIT) {
+    // the owned w (cw) copies of this tile, issued at its start, have normally landed by now
+    const bool ok_o = mbar_wait_bounded(bar_o, par_o);
+    if (__syncthreads_or(!ok_o)) return false;
+  } else {
+    __syncthreads();   // (the owned boxes came with the region, on its barrier)
+  }
 
   // the node phase's parameters in registers: when prm lives in shared memory (the
   // batched kernel), every store through an output pointer would otherwise force
@@ -522,32 +563,37 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
       if (a_out) a_out[n + h] = h ? make_float2(acc.z, acc.w) : make_float2(acc.x, acc.y);
     }
   }
-  __syncthreads();   // stage s and the exchange buffers are free again
+  __syncthreads();   // stage s, the owned buffer and the exchange buffers are free again
   return true;
 }
 
-template <int P, int TE, int NT, bool KAHAN>
-__global__ void __launch_bounds__(NT, min_blocks(Layout<P, TE, KAHAN>::TOTAL))
+template <int P, int TE, int NT, bool KAHAN, int NOB = owned_buffers(P),
+          int MINB = min_blocks(Layout<P, TE, KAHAN, NOB>::TOTAL)>
+__global__ void __launch_bounds__(NT, MINB)
 persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ CUtensorMap tm_cu,
              const __grid_constant__ CUtensorMap tm_w, const __grid_constant__ CUtensorMap tm_cw,
              const Params prm)
 {
   typedef Geo<P, TE> G;
-  typedef Layout<P, TE, KAHAN> L;
+  typedef Layout<P, TE, KAHAN, NOB> L;
   constexpr int N1 = G::N1, NEX = G::NEX;
   static_assert(NT >= G::ITEMS, "one (element, line) item per thread");
+  static_assert(NOB == 1 || NOB == 2, "one or two owned-box buffers");
   const float *W = c_w[P - 1];
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char *stage0 = smem;
   unsigned char *stage1 = smem + L::STAGE;
-  float2 *X1 = reinterpret_cast<float2 *>(smem + 2 * L::STAGE);             // eta derivatives, then element forces
-  float2 *X2 = reinterpret_cast<float2 *>(smem + 2 * L::STAGE + L::XCH);     // eta fluxes
-  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * L::STAGE + 2 * L::XCH);
-  const uint32_t bar0 = smem_u32(&bars[0]), bar1 = smem_u32(&bars[1]);
+  unsigned char *ob0 = smem + 2 * L::STAGE;                                             // owned w (cw)
+  unsigned char *ob1 = ob0 + (NOB - 1) * L::OWNB;
+  float2 *X1 = reinterpret_cast<float2 *>(smem + 2 * L::STAGE + NOB * L::OWNB);          // eta derivatives, then element forces
+  float2 *X2 = reinterpret_cast<float2 *>(smem + 2 * L::STAGE + NOB * L::OWNB + L::XCH); // eta fluxes
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * L::STAGE + NOB * L::OWNB + 2 * L::XCH);
+  const uint32_t bar0 = smem_u32(&bars[0]), bar1 = smem_u32(&bars[1]), bo0 = smem_u32(&bars[2]);
 
   if (threadIdx.x == 0) {
     mbar_init(bar0, 1);
     mbar_init(bar1, 1);
+    mbar_init(bo0, 1);
     fence_barrier_init();
     prefetch_map(&tm_u); prefetch_map(&tm_w);
     if (KAHAN) { prefetch_map(&tm_cu); prefetch_map(&tm_cw); }
@@ -565,24 +611,40 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
   int t = blockIdx.x;
   int tx = t % prm.ntx, ty = t / prm.ntx;
   const int dtx = gridDim.x % prm.ntx, dty = gridDim.x / prm.ntx;
-  if (t < prm.ntiles && threadIdx.x == 0) issue_tile<P, TE, KAHAN>(tx, ty, stage0, bar0, &tm_u, &tm_cu, &tm_w, &tm_cw);
+  if (t < prm.ntiles && threadIdx.x == 0) {
+    if (NOB == 2) issue_both<P, TE, KAHAN>(tx, ty, stage0, ob0, bar0, &tm_u, &tm_cu, &tm_w, &tm_cw);
+    else issue_region<P, TE, KAHAN>(tx, ty, stage0, bar0, &tm_u, &tm_cu);
+  }
   for (int it = 0; t < prm.ntiles; it++, t += gridDim.x) {
     const int s = it & 1;
     const uint32_t bar = s ? bar1 : bar0;
     const uint32_t parity = (it >> 1) & 1;
     int txn = tx + dtx, tyn = ty + dty;
     if (txn >= prm.ntx) { txn -= prm.ntx; tyn++; }
-    // prefetch the next tile into the other stage (freed by the barrier that ended the previous tile)
+    // this tile's owned w (cw) with one owned buffer, the next tile's with two, and the
+    // next tile's region into the other stage (each buffer was freed by the barrier
+    // that ended the previous tile)
     const int tn = t + gridDim.x;
-    if (threadIdx.x == 0 && tn < prm.ntiles) {
+    unsigned char *ob = (NOB == 2 && s) ? ob1 : ob0;
+    const uint32_t par_o = (uint32_t)(it & 1);   // the owned barrier (one owned buffer)
+    if (threadIdx.x == 0) {
       fence_proxy_async();
-      issue_tile<P, TE, KAHAN>(txn, tyn, s ? stage0 : stage1, s ? bar0 : bar1, &tm_u, &tm_cu, &tm_w, &tm_cw);
+      if (NOB == 1) issue_owned<P, TE, KAHAN>(tx, ty, ob0, bo0, &tm_w, &tm_cw);
+      if (tn < prm.ntiles) {
+        if (NOB == 2)
+          issue_both<P, TE, KAHAN>(txn, tyn, s ? stage0 : stage1, s ? ob0 : ob1, s ? bar0 : bar1, &tm_u, &tm_cu, &tm_w,
+                                   &tm_cw);
+        else
+          issue_region<P, TE, KAHAN>(txn, tyn, s ? stage0 : stage1, s ? bar0 : bar1, &tm_u, &tm_cu);
+      }
     }
-    if (!tile_body<P, TE, NT, KAHAN>(prm, tx, ty, s ? stage1 : stage0, bar, parity, X1, X2, item, el, j, ecx, ecy, wj)) {
+    if (!tile_body<P, TE, NT, KAHAN, NOB == 1>(prm, tx, ty, s ? stage1 : stage0, bar, parity, ob, bo0, par_o, X1, X2,
+                                               item, el, j, ecx, ecy, wj)) {
       if (threadIdx.x == 0) {
         atomicExch(prm.err, 1);
         // let this CTA's copies in flight land before the shared memory is released
         mbar_wait_bounded(bar, parity);
+        if (NOB == 1) mbar_wait_bounded(bo0, par_o);
         if (tn < prm.ntiles) mbar_wait_bounded(s ? bar0 : bar1, ((it + 1) >> 1) & 1);
       }
       return;
@@ -618,30 +680,35 @@ __device__ __forceinline__ void copy_params_async(Params *dst, const Params *src
   asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
-template <int P, int TE, int NT, bool KAHAN>
-__global__ void __launch_bounds__(NT, min_blocks(Layout<P, TE, KAHAN>::BATCH_TOTAL))
+template <int P, int TE, int NT, bool KAHAN, int NOB = owned_buffers(P),
+          int MINB = min_blocks(Layout<P, TE, KAHAN, NOB>::BATCH_TOTAL)>
+__global__ void __launch_bounds__(NT, MINB)
 persist_batch(const BatchArgs ba)
 {
   typedef Geo<P, TE> G;
-  typedef Layout<P, TE, KAHAN> L;
+  typedef Layout<P, TE, KAHAN, NOB> L;
   constexpr int N1 = G::N1, NEX = G::NEX;
   static_assert(NT >= G::ITEMS, "one (element, line) item per thread");
+  static_assert(NOB == 1 || NOB == 2, "one or two owned-box buffers");
   static_assert(sizeof(Params) % 16 == 0 && sizeof(Params) / 16 <= 32, "Params copied in 16-byte pieces by one warp");
   const float *W = c_w[P - 1];
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char *stage0 = smem;
   unsigned char *stage1 = smem + L::STAGE;
-  float2 *X1 = reinterpret_cast<float2 *>(smem + 2 * L::STAGE);
-  float2 *X2 = reinterpret_cast<float2 *>(smem + 2 * L::STAGE + L::XCH);
-  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * L::STAGE + 2 * L::XCH);
-  const uint32_t bar0 = smem_u32(&bars[0]), bar1 = smem_u32(&bars[1]);
+  unsigned char *ob0 = smem + 2 * L::STAGE;
+  unsigned char *ob1 = ob0 + (NOB - 1) * L::OWNB;
+  float2 *X1 = reinterpret_cast<float2 *>(smem + 2 * L::STAGE + NOB * L::OWNB);
+  float2 *X2 = reinterpret_cast<float2 *>(smem + 2 * L::STAGE + NOB * L::OWNB + L::XCH);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * L::STAGE + NOB * L::OWNB + 2 * L::XCH);
+  const uint32_t bar0 = smem_u32(&bars[0]), bar1 = smem_u32(&bars[1]), bo0 = smem_u32(&bars[2]);
   // two slots for the shot parameters of the current and the next tile (this step's pointers patched in)
   Params *slot0 = reinterpret_cast<Params *>(smem + L::TOTAL);
-  Params *slot1 = reinterpret_cast<Params *>(smem + L::TOTAL + al128(sizeof(Params)));
+  Params *slot1 = reinterpret_cast<Params *>(smem + L::TOTAL + sizeof(Params));
 
   if (threadIdx.x == 0) {
     mbar_init(bar0, 1);
     mbar_init(bar1, 1);
+    mbar_init(bo0, 1);
     fence_barrier_init();
   }
   __syncthreads();
@@ -660,8 +727,9 @@ persist_batch(const BatchArgs ba)
   // Per-tile pipeline.  Every thread keeps the work items of this tile and the next
   // in registers (the list entry two tiles ahead is loaded one tile early).  The
   // next tile's shot parameters are copied into the other parameter slot with
-  // cp.async by warp 0 while this tile is computed, and its TMA copies are issued
-  // at the top of this tile, so no dependent global load sits between two tiles.
+  // cp.async by warp 0 while this tile is computed; its region copies and this tile's
+  // owned copies are issued at the top of this tile, so no dependent global load sits
+  // between two tiles.
   const int stride = gridDim.x;
   int w = blockIdx.x;
   int2 cur = make_int2(0, 0), nxt = make_int2(0, 0);
@@ -670,7 +738,8 @@ persist_batch(const BatchArgs ba)
   if (w < ba.nitems) {
     if (threadIdx.x == 0) {
       const CUtensorMap *m = ba.maps + 4 * cur.x;
-      issue_tile<P, TE, KAHAN>(cur.y & 0xFFFF, cur.y >> 16, stage0, bar0, m, m + 1, m + 2, m + 3);
+      if (NOB == 2) issue_both<P, TE, KAHAN>(cur.y & 0xFFFF, cur.y >> 16, stage0, ob0, bar0, m, m + 1, m + 2, m + 3);
+      else issue_region<P, TE, KAHAN>(cur.y & 0xFFFF, cur.y >> 16, stage0, bar0, m, m + 1);
     }
     if (threadIdx.x < 32) copy_params_async(slot0, ba.shots + cur.x);
   }
@@ -680,6 +749,8 @@ persist_batch(const BatchArgs ba)
     const uint32_t parity = (it >> 1) & 1;
     const int wn = w + stride;
     Params &sp = s ? *slot1 : *slot0;
+    unsigned char *ob = (NOB == 2 && s) ? ob1 : ob0;
+    const uint32_t par_o = (uint32_t)(it & 1);   // the owned barrier (one owned buffer)
     const int2 nn = (wn + stride < ba.nitems) ? ba.items[wn + stride] : make_int2(0, 0);   // for the next tile
     if (threadIdx.x < 32) {
       cp_async_wait_all();
@@ -689,22 +760,30 @@ persist_batch(const BatchArgs ba)
         sp.stf = sp.stf + (size_t)ba.kblk * sp.nsrc;
         sp.rbuf_out = const_cast<float *>(batch_rbuf(sp, ba.kblk));
         if (!ba.write_a) sp.a_out = nullptr;
+        fence_proxy_async();
+        if (NOB == 1) {
+          const CUtensorMap *mc = ba.maps + 4 * cur.x;
+          issue_owned<P, TE, KAHAN>(cur.y & 0xFFFF, cur.y >> 16, ob0, bo0, mc + 2, mc + 3);
+        }
         if (wn < ba.nitems) {
-          fence_proxy_async();
           const CUtensorMap *m = ba.maps + 4 * nxt.x;
-          issue_tile<P, TE, KAHAN>(nxt.y & 0xFFFF, nxt.y >> 16, s ? stage0 : stage1, s ? bar0 : bar1, m, m + 1,
-                                   m + 2, m + 3);
+          if (NOB == 2)
+            issue_both<P, TE, KAHAN>(nxt.y & 0xFFFF, nxt.y >> 16, s ? stage0 : stage1, s ? ob0 : ob1, s ? bar0 : bar1, m,
+                                     m + 1, m + 2, m + 3);
+          else
+            issue_region<P, TE, KAHAN>(nxt.y & 0xFFFF, nxt.y >> 16, s ? stage0 : stage1, s ? bar0 : bar1, m, m + 1);
         }
       }
     }
     __syncthreads();   // slot s is complete; every thread has left the previous tile, so the other slot is free
     if (threadIdx.x < 32 && wn < ba.nitems) copy_params_async(s ? slot0 : slot1, ba.shots + nxt.x);
-    if (!tile_body<P, TE, NT, KAHAN>(sp, cur.y & 0xFFFF, cur.y >> 16, s ? stage1 : stage0, bar, parity, X1, X2, item,
-                                     el, j, ecx, ecy, wj)) {
+    if (!tile_body<P, TE, NT, KAHAN, NOB == 1>(sp, cur.y & 0xFFFF, cur.y >> 16, s ? stage1 : stage0, bar, parity, ob,
+                                               bo0, par_o, X1, X2, item, el, j, ecx, ecy, wj)) {
       if (threadIdx.x < 32) cp_async_wait_all();
       if (threadIdx.x == 0) {
         atomicExch(ba.err, 1);
         mbar_wait_bounded(bar, parity);
+        if (NOB == 1) mbar_wait_bounded(bo0, par_o);
         if (wn < ba.nitems) mbar_wait_bounded(s ? bar0 : bar1, ((it + 1) >> 1) & 1);
       }
       return;

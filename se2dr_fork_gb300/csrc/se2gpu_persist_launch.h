@@ -9,6 +9,7 @@ namespace se2p {
 
 struct TileShape {
   int tex, tey, nt, region_w, region_h, own_w, own_h;
+  int owned_buffers;   // 2: the next tile's owned boxes arrive a tile ahead; 1: during the tile
   size_t smem;
 };
 

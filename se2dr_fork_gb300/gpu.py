@@ -24,7 +24,7 @@ PRECISIONS = {"fp64": FP64, "fp32_kahan": FP32_KAHAN, "fp32": FP32}
 EXPORTS = ["se2gpu_create", "se2gpu_destroy", "se2gpu_last_error", "se2gpu_create_error", "se2gpu_set_stream",
            "se2gpu_synchronize", "se2gpu_set_fields", "se2gpu_get_fields", "se2gpu_advance", "se2gpu_traces",
            "se2gpu_norms", "se2gpu_assemble_linear_form", "se2gpu_assemble_linear_form_device", "se2gpu_info",
-           "se2gpu_device_fields", "se2gpu_tile_configs", "se2gpu_set_tile_config",
+           "se2gpu_device_fields", "se2gpu_tile_configs", "se2gpu_tile_config_info", "se2gpu_set_tile_config",
            "se2gpu_ensemble_create", "se2gpu_ensemble_destroy", "se2gpu_ensemble_last_error",
            "se2gpu_ensemble_set_stream", "se2gpu_ensemble_set_graphs", "se2gpu_ensemble_set_tile_config",
            "se2gpu_ensemble_tile_config", "se2gpu_ensemble_advance", "se2gpu_ensemble_enqueue",
@@ -73,6 +73,7 @@ def lib():
         L.se2gpu_info.argtypes = [vp, C.POINTER(C.c_long)]
         L.se2gpu_device_fields.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]
         L.se2gpu_tile_configs.argtypes = [vp, _ip, _ip, C.c_int]
+        L.se2gpu_tile_config_info.argtypes = [vp, C.c_int, _ip]
         L.se2gpu_set_tile_config.argtypes = [vp, C.c_int]
         L.se2gpu_ensemble_create.argtypes = [C.POINTER(_CProblem), C.c_int, C.c_int, C.c_int, C.POINTER(vp)]
         L.se2gpu_ensemble_destroy.argtypes = [vp]
@@ -249,6 +250,13 @@ class Solver:
         t = np.zeros(16, dtype=np.int32)
         n = self._check(lib().se2gpu_tile_configs(self._h, _p(e, _ip), _p(t, _ip), 16), "se2gpu_tile_configs")
         return [(int(e[i]), int(t[i])) for i in range(n)]
+
+    def tile_config_info(self, config: int) -> dict:
+        """One configuration in full (se2gpu_tile_config_info)."""
+        info = np.zeros(4, dtype=np.int32)
+        self._check(lib().se2gpu_tile_config_info(self._h, int(config), _p(info, _ip)), "se2gpu_tile_config_info")
+        return {"edge": int(info[0]), "threads": int(info[1]), "owned_buffers": int(info[2]),
+                "ctas_per_sm": int(info[3])}
 
     def set_tile_config(self, config: int):
         self._check(lib().se2gpu_set_tile_config(self._h, int(config)), "se2gpu_set_tile_config")
