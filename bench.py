@@ -46,7 +46,7 @@ def peaks():
 # dram__bytes_write.sum of one launch at 1024^2, degree 4, divided by its 16.79M nodes; the
 # kernel's traffic grows in proportion to the nodes, so it is scaled to the workload's node
 # count): profiles/persist_step_fp32kahan_grf1024.md, profiles/step_kernel_fp64_grf512.md
-MEASURED_TRAFFIC_PER_NODE = {"fp32_kahan": 1109.6e6 / 16785409}
+MEASURED_TRAFFIC_PER_NODE = {"fp32_kahan": 1120.2e6 / 16785409}
 
 
 def alg_bytes_per_node(precision: str, ne: int, nnodes: int) -> float:

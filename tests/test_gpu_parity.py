@@ -283,6 +283,23 @@ def test_fp32_tile_configs_agree(p, precision):
             assert all(np.array_equal(x, y) for x, y in zip(out, ref)), c
 
 
+@pytest.mark.parametrize("p", [1, 3, 4, 8])
+def test_tile_config_info(p):
+    """se2gpu_tile_config_info agrees with se2gpu_tile_configs and reports one or two owned
+    buffers and at least one resident CTA per SM for every FP32 configuration."""
+    setup = H.Setup(S.demo(9, 7, p=p, tmax=1.0).replace(nt=4, nearest_internal_gll=(p > 1)))
+    sol = G.Solver(setup, "fp32_kahan")
+    cfgs = sol.tile_configs()
+    for c, (edge, threads) in enumerate(cfgs):
+        info = sol.tile_config_info(c)
+        assert (info["edge"], info["threads"]) == (edge, threads)
+        assert info["owned_buffers"] in (1, 2) and 1 <= info["ctas_per_sm"] <= 3, info
+    with pytest.raises(G.GpuError):
+        sol.tile_config_info(len(cfgs))
+    f64 = G.Solver(setup, "fp64").tile_config_info(0)
+    assert f64["owned_buffers"] == 0 and f64["ctas_per_sm"] == 0
+
+
 @pytest.mark.parametrize("precision", ["fp64", "fp32_kahan", "fp32"])
 def test_checkpoint_resume_is_bitwise(precision):
     """Stop after 37 steps, checkpoint, resume in a new handle: identical traces and fields."""
