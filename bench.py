@@ -476,6 +476,11 @@ def run_surrogate(args):
                         "accepted_misfit_mean": float(mis[acc].mean()) if acc.any() else None})
     served = SU.serve(nets, dtest, test.specs, threshold=args.threshold, audit=0.05)
     solver_sps = dtest.n / test.wall_seconds
+    # the gain at equal misfit: coarser solvers on the in-distribution held-out draws
+    ladder = SU.solver_ladder(te_in.specs, te_in.traces)
+    sur_sps = dtest.n / t_pred
+    eq = SU.equal_misfit(ladder, float(mis[~is_ood].mean()), sur_sps)
+    log(f"equal misfit: {eq}")
     line = {"metric": "seismograms/s surrogate vs solver @1% L2", "value": served["seismograms_per_s"],
             "unit": "seismograms/s", "n_gpus": 1, "higher_is_better": True, "dtype": "bf16", "data": "synthetic",
             "config": {"workload": f"{args.train} training draws, {args.test} held-out + {nood} out-of-distribution "
@@ -492,6 +497,10 @@ def run_surrogate(args):
                          "disagreement_mean": float(dis[~is_ood].mean()), "ood_disagreement_mean": float(dis[is_ood].mean()),
                          "corr_disagreement_misfit": float(np.corrcoef(dis, mis)[0, 1])},
             "what_if": what_if,
+            "equal_misfit": {"surrogate_misfit_mean": float(mis[~is_ood].mean()),
+                             "surrogate_draws_per_s": sur_sps, "fine_solver_draws_per_s": solver_sps,
+                             "solver_ladder": ladder, "solver_at_equal_misfit": eq["solver"],
+                             "gain_at_equal_misfit": eq["gain"]},
             "training": {"samples_per_s": [st["samples_per_s"] for st in stats],
                          "tflops": [3 * fwd * st["samples_per_s"] / 1e12 for st in stats],
                          "final_loss": [st["loss"][-1] for st in stats], "loss_curve_member0": stats[0]["loss"]},

@@ -73,14 +73,14 @@ class Dataset:
         return self.materials.shape[0]
 
 
-def _traces_from_rows(rows: np.ndarray) -> np.ndarray:
-    """[steps, 1 + 7 nrec] receiver rows -> [nrec, 2 * NSAMP] velocities every DECIMATE-th step."""
-    sel = rows[DECIMATE - 1::DECIMATE, 1:].reshape(-1, NREC, 7)[:NSAMP]
+def _traces_from_rows(rows: np.ndarray, decimate: int = DECIMATE) -> np.ndarray:
+    """[steps, 1 + 7 nrec] receiver rows -> [nrec, 2 * NSAMP] velocities every decimate-th step."""
+    sel = rows[decimate - 1::decimate, 1:].reshape(-1, NREC, 7)[:NSAMP]
     return np.concatenate([sel[:, :, 2].T, sel[:, :, 3].T], axis=1).astype(np.float32)
 
 
 def solve(specs: List[S.Spec], precision: str = "fp32_kahan", chunk: int = 1000, block: int = 128,
-          threads: int = 16):
+          threads: int = 16, nsteps: int = NSTEPS, decimate: int = DECIMATE):
     """Solve the draws with the batched FP32 solver; returns ([n, 16, 2048] traces, solver seconds)."""
     out = np.zeros((len(specs), NREC, 2 * NSAMP), dtype=np.float32)
     secs = 0.0
@@ -90,11 +90,11 @@ def solve(specs: List[S.Spec], precision: str = "fp32_kahan", chunk: int = 1000,
             setups = list(ex.map(H.Setup, part))
             t0 = time.perf_counter()
             ens = G.Ensemble(setups, precision, block=block)
-            rows = ens.advance(NSTEPS)
+            rows = ens.advance(nsteps)
             ens.close()
             secs += time.perf_counter() - t0
             for i, r in enumerate(rows):
-                out[c0 + i] = _traces_from_rows(r)
+                out[c0 + i] = _traces_from_rows(r, decimate)
             del setups, rows
     return out, secs
 
@@ -125,6 +125,58 @@ def concat(*ds: Dataset) -> Dataset:
     return Dataset(np.concatenate([d.materials for d in ds]), np.concatenate([d.src for d in ds]),
                    np.concatenate([d.traces for d in ds]), np.concatenate([d.kind for d in ds]),
                    sum(d.seconds for d in ds), sum(d.wall_seconds for d in ds), specs)
+
+
+# Coarser solvers for the comparison at equal misfit: (elements per side, degree).  Each
+# runs the same draw on the same 4 km square with block-averaged cell materials, the same
+# source, wavelet and receivers, and the largest time step r * dt (r = 1, 2 or 4) within
+# 0.5 x its CFL step at Vp = 7500 m/s, so its samples fall on the same times.
+LADDER = [(64, 4), (64, 3), (64, 2), (32, 4), (32, 3), (32, 2), (16, 4), (16, 2)]
+
+
+def coarse_spec(sp: S.Spec, mx: int, p: int, dt: float):
+    """(the draw on mx x mx elements of degree p, time-step ratio r)."""
+    f = GRID // mx
+    if f * mx != GRID:
+        raise ValueError(f"{mx} does not divide {GRID}")
+
+    def avg(a):
+        return np.asarray(a, dtype=np.float64).reshape(mx, f, mx, f).mean(axis=(1, 3)).ravel()
+
+    probe = S.Spec(mx=mx, my=mx, p=p, scale=(GRID * CELL, GRID * CELL), shift=(0.0, 0.0), vp=7500.0,
+                   vs=7500.0 / 1.6, rho=2500.0, cfl=0.5, tmax=1.0e30, nt=1)
+    dt_max = H.Setup(probe).dt
+    r = max(k for k in (1, 2, 4) if k * dt <= dt_max * (1.0 + 1e-12))
+    return sp.replace(mx=mx, my=mx, p=p, cell_vp=avg(sp.cell_vp), cell_vs=avg(sp.cell_vs), cell_rho=avg(sp.cell_rho),
+                      dt=r * dt, nt=NSTEPS // r), r
+
+
+def solver_ladder(specs: List[S.Spec], true: np.ndarray, ladder=LADDER, threads: int = 16) -> List[dict]:
+    """Misfit against `true` (the draws' fine traces) and throughput of each coarser solver."""
+    dt = specs[0].dt
+    out = []
+    for mx, p in ladder:
+        t0 = time.perf_counter()
+        cs = [coarse_spec(sp, mx, p, dt) for sp in specs]
+        r = cs[0][1]
+        tr, secs = solve([c for c, _ in cs], chunk=len(cs), threads=threads, nsteps=NSTEPS // r, decimate=DECIMATE // r)
+        wall = time.perf_counter() - t0
+        mis = rel_l2(tr, true)
+        nodes = (p * mx + 1) ** 2
+        out.append({"mx": mx, "p": p, "dt_ratio": r, "nodes": nodes, "solver_seconds": secs, "wall_seconds": wall,
+                    "draws_per_s": len(specs) / wall, "misfit_mean": float(mis.mean()),
+                    "misfit_median": float(np.median(mis)), "misfit_p90": float(np.percentile(mis, 90))})
+    return out
+
+
+def equal_misfit(ladder: List[dict], misfit: float, draws_per_s: float) -> dict:
+    """The fastest ladder solver whose mean misfit is at most `misfit`, and the gain of a method of
+    that misfit and throughput over it (None when no coarser solver is that accurate)."""
+    ok = [e for e in ladder if e["misfit_mean"] <= misfit]
+    if not ok:
+        return {"solver": None, "gain": None}
+    best = max(ok, key=lambda e: e["draws_per_s"])
+    return {"solver": best, "gain": draws_per_s / best["draws_per_s"]}
 
 
 def rel_l2(pred: np.ndarray, true: np.ndarray) -> np.ndarray:

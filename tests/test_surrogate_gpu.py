@@ -42,3 +42,19 @@ def test_short_training_run_fits_and_predicts():
     assert st["loss"][-1] < st["loss"][0]
     preds = SU.predict([net], data, np.arange(8))
     assert preds.shape == (1, 8, 16, 2048) and np.all(np.isfinite(preds))
+
+
+def test_solver_ladder_and_equal_misfit():
+    """The coarse-solver ladder behind the comparison at equal misfit: the fine configuration
+    itself reproduces the draws' traces exactly, coarser ones cost less per draw and miss more."""
+    specs = SU.specs_of(21, 3)
+    true, _ = SU.solve(specs, chunk=3)
+    lad = SU.solver_ladder(specs, true, ladder=[(SU.GRID, 4), (64, 4), (32, 2)])
+    fine, mid, coarse = lad
+    assert fine["dt_ratio"] == 1 and fine["misfit_mean"] == 0.0
+    assert mid["dt_ratio"] == 2 and coarse["dt_ratio"] == 4
+    assert 0.0 < mid["misfit_mean"] < coarse["misfit_mean"] and np.isfinite(coarse["misfit_mean"])
+    assert coarse["nodes"] < mid["nodes"] < fine["nodes"]
+    eq = SU.equal_misfit(lad, mid["misfit_mean"], 1.0)
+    assert eq["solver"]["misfit_mean"] <= mid["misfit_mean"] and eq["gain"] == 1.0 / eq["solver"]["draws_per_s"]
+    assert SU.equal_misfit(lad, -1.0, 1.0) == {"solver": None, "gain": None}
