@@ -31,12 +31,22 @@
 
 namespace {
 
+// a launch covers up to SE2P_BATCH_SHOTS consecutive shots of a group (their parameters
+// are the kernel's parameter)
+struct Chunk {
+  int first = 0, nshots = 0;     // shots [first, first + nshots) of the group
+  int item_off = 0, nitems = 0;  // its work list inside the group's
+  int grid = 1;
+};
+
 struct Group {
-  int p = 0, config = 0, grid = 1, nitems = 0;
+  int p = 0, config = 0, nitems = 0;
   std::vector<int> shots;                  // ensemble shot indices, ascending
+  std::vector<Chunk> chunks;
   se2p::Params *tab[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};   // [input buffer][slot], device
+  std::vector<se2p::Params> htab[2][2];                                // the same, host (launch arguments)
   CUtensorMap *maps[2] = {nullptr, nullptr};                           // [input buffer], device [shot][4]
-  int2 *items = nullptr;                                               // device (local shot, ty << 16 | tx)
+  int2 *items = nullptr;                                               // device (shot in its chunk, ty << 16 | tx)
 };
 
 }  // namespace
@@ -92,11 +102,18 @@ static void drop_graphs(se2gpu_ensemble *e)
 static void free_group(Group &g)
 {
   for (int c = 0; c < 2; c++) {
-    for (int s = 0; s < 2; s++) cudaFree(g.tab[c][s]);
+    for (int s = 0; s < 2; s++) {
+      cudaFree(g.tab[c][s]);
+      g.tab[c][s] = nullptr;
+      g.htab[c][s].clear();
+    }
     cudaFree(g.maps[c]);
+    g.maps[c] = nullptr;
   }
   cudaFree(g.items);
-  g = Group{g.p, g.config, g.grid, 0, g.shots};
+  g.items = nullptr;
+  g.nitems = 0;
+  g.chunks.clear();
 }
 
 extern "C" void se2gpu_ensemble_destroy(se2gpu_ensemble *e)
@@ -160,6 +177,7 @@ static int build_group(se2gpu_ensemble *e, Group &g)
       }
       int rc = dput(e, &g.tab[c][sl], tab.data(), tab.size());
       if (rc) return rc;
+      g.htab[c][sl] = tab;
     }
   for (int c = 0; c < 2; c++) {
     for (int i = 0; i < ns; i++)
@@ -167,17 +185,25 @@ static int build_group(se2gpu_ensemble *e, Group &g)
     int rc = dput(e, &g.maps[c], maps.data(), maps.size());
     if (rc) return rc;
   }
-  for (int i = 0; i < ns; i++) {
-    se2gpu_solver *h = e->sol[g.shots[i]];
-    if (h->pntx >= 32768 || h->pnty >= 32768) return efail(e, SE2GPU_ERR_ARG, "shot %d: more than 32767 tiles along an axis", g.shots[i]);
-    for (int t = 0; t < h->pntx * h->pnty; t++) items.push_back(make_int2(i, ((t / h->pntx) << 16) | (t % h->pntx)));
+  g.config = e->sol[g.shots[0]]->pconfig;
+  const int occ = std::max(1, se2p::occupancy(g.p, g.config, e->kahan, true));
+  for (int f = 0; f < ns; f += SE2P_BATCH_SHOTS) {
+    Chunk ch;
+    ch.first = f;
+    ch.nshots = std::min(SE2P_BATCH_SHOTS, ns - f);
+    ch.item_off = (int)items.size();
+    for (int i = f; i < f + ch.nshots; i++) {
+      se2gpu_solver *h = e->sol[g.shots[i]];
+      if (h->pntx >= 32768 || h->pnty >= 32768) return efail(e, SE2GPU_ERR_ARG, "shot %d: more than 32767 tiles along an axis", g.shots[i]);
+      for (int t = 0; t < h->pntx * h->pnty; t++) items.push_back(make_int2(i - f, ((t / h->pntx) << 16) | (t % h->pntx)));
+    }
+    ch.nitems = (int)items.size() - ch.item_off;
+    ch.grid = std::max(1, std::min(ch.nitems, occ * e->nsm));
+    g.chunks.push_back(ch);
   }
   g.nitems = (int)items.size();
   int rc = dput(e, &g.items, items.data(), items.size());
   if (rc) return rc;
-  g.config = e->sol[g.shots[0]]->pconfig;
-  const int occ = std::max(1, se2p::occupancy(g.p, g.config, e->kahan, true));
-  g.grid = std::max(1, std::min(g.nitems, occ * e->nsm));
   return 0;
 }
 
@@ -309,19 +335,21 @@ static int enqueue_block(se2gpu_ensemble *e, int cur, int sl, int n, cudaStream_
 {
   for (int k = 0; k < n; k++) {
     const int cin = cur ^ (k & 1);
-    for (Group &g : e->groups) {
-      se2p::BatchArgs ba;
-      ba.shots = g.tab[cin][sl];
-      ba.maps = g.maps[cin];
-      ba.items = g.items;
-      ba.nshots = (int)g.shots.size();
-      ba.nitems = g.nitems;
-      ba.kblk = k;
-      ba.write_a = (k == n - 1) ? 1 : 0;
-      ba.err = e->err_dev;
-      cudaError_t r = se2p::launch_batch(g.p, g.config, e->kahan, ba, g.grid, st);
-      if (r != cudaSuccess) return efail(e, SE2GPU_ERR_CUDA, "batched step kernel (degree %d): %s", g.p, cudaGetErrorString(r));
-    }
+    for (Group &g : e->groups)
+      for (const Chunk &ch : g.chunks) {
+        static thread_local se2p::BatchArgs ba;   // 28 KB: kept off the stack
+        ba.maps = g.maps[cin] + 4 * (size_t)ch.first;
+        ba.items = g.items + ch.item_off;
+        ba.nshots = ch.nshots;
+        ba.nitems = ch.nitems;
+        ba.kblk = k;
+        ba.write_a = (k == n - 1) ? 1 : 0;
+        ba.err = e->err_dev;
+        memcpy(ba.shots, g.htab[cin][sl].data() + ch.first, sizeof(se2p::Params) * ch.nshots);
+        cudaError_t r = se2p::launch_batch(g.p, g.config, e->kahan, ba, ch.grid, st);
+        if (r != cudaSuccess)
+          return efail(e, SE2GPU_ERR_CUDA, "batched step kernel (degree %d): %s", g.p, cudaGetErrorString(r));
+      }
   }
   for (Group &g : e->groups) {
     cudaError_t r = se2p::launch_record_batch(g.p, g.tab[cur][sl], (int)g.shots.size(), n - 1, st);
@@ -330,7 +358,12 @@ static int enqueue_block(se2gpu_ensemble *e, int cur, int sl, int n, cudaStream_
   return 0;
 }
 
-static int launches_per_block(const se2gpu_ensemble *e, int n) { return (int)e->groups.size() * (n + 1); }
+static int launches_per_block(const se2gpu_ensemble *e, int n)
+{
+  int k = 0;
+  for (const Group &g : e->groups) k += (int)g.chunks.size() * n + 1;
+  return k;
+}
 
 static int run_block(se2gpu_ensemble *e, int sl, int n)
 {

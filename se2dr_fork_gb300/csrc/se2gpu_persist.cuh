@@ -143,9 +143,7 @@ struct Layout {
   static constexpr size_t XCH = al128(sizeof(float2) * G::NE * G::XS);    // exchange buffer
   static constexpr size_t MISC = 64;
   static constexpr size_t TOTAL = 2 * STAGE + NOB * OWNB + 2 * XCH + MISC;
-  // the batched kernel keeps the shot parameters of the current and the next tile right
-  // after the barriers (MISC): two 16-byte aligned slots
-  static constexpr size_t BATCH_TOTAL = TOTAL + al128(2 * sizeof(Params));
+  static constexpr size_t BATCH_TOTAL = TOTAL;   // the batched kernel's shot parameters are a kernel parameter
   static constexpr uint32_t TX_REGION = (uint32_t)((KAHAN ? 2 : 1) * sizeof(float2) * G::BXW * G::BXH);
   static constexpr uint32_t TX_OWNED = (uint32_t)((KAHAN ? 2 : 1) * sizeof(float2) * G::OBW * G::OBH);
 };
@@ -252,10 +250,18 @@ __device__ void sample_rows(const Params &prm, const float *rbuf_in, double *tra
   }
 }
 
+// the pointers of one step of a tile's shot: this step's source values, the receiver
+// side buffer it writes and the optional a_k output (null: not written)
+struct StepPtrs {
+  const double *stf;
+  float *rbuf_out;
+  float2 *a_out;
+};
+
 // one tile: prefetch of global values, wait for the tile's copies, the three
 // element phases and the node phase.  Returns false when the bounded wait expired.
 template <int P, int TE, int NT, bool KAHAN, bool OWAIT>
-__device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, const unsigned char *st, uint32_t bar,
+__device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp, int tx, int ty, const unsigned char *st, uint32_t bar,
                                           uint32_t parity, const unsigned char *ob, uint32_t bar_o, uint32_t par_o,
                                           float2 *X1, float2 *X2, int item, int el, int j, int ecx, int ecy, float wj)
 {
@@ -414,7 +420,7 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
   // batched kernel), every store through an output pointer would otherwise force
   // the following parameter reads to be repeated
   float2 *const u_out = prm.u_out, *const w_out = prm.w_out, *const cu_out = prm.cu_out, *const cw_out = prm.cw_out;
-  float2 *const a_out = prm.a_out;
+  float2 *const a_out = stp.a_out;
   const int pitch = prm.pitch, NXP = prm.mx * P, NYP = prm.my * P;
   const float dt = prm.dt, half_dt = prm.half_dt;
   // ---- owned nodes: ordered element sum, sources, update
@@ -440,7 +446,7 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
         const int sidx = prm.tile_src_idx[q], se = prm.src_elem[sidx], sx = se % prm.mx, sy = se / prm.mx;
         const int a = X - sx * P, bb = Y - sy * P;
         if (a >= 0 && a <= P && bb >= 0 && bb <= P) {
-          const float val = (float)prm.stf[sidx];
+          const float val = (float)stp.stf[sidx];
           const float *sv = prm.src_vals + (size_t)sidx * 2 * NPE + 2 * (a + bb * N1);
           fx = fmaf(val, sv[0], fx); fy = fmaf(val, sv[1], fy);
         }
@@ -454,7 +460,7 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
         const int r = prm.tile_rec_idx[q], re = prm.rec_elem[r], rx = re % prm.mx, ry = re / prm.mx;
         const int a = X - rx * P, bb = Y - ry * P;
         if (a >= 0 && a <= P && bb >= 0 && bb <= P) {
-          float *rb = prm.rbuf_out + ((size_t)r * NPE + a + bb * N1) * 6;
+          float *rb = stp.rbuf_out + ((size_t)r * NPE + a + bb * N1) * 6;
           rb[0] = u.x; rb[1] = u.y; rb[2] = fmaf(half_dt, acc.x, w.x); rb[3] = fmaf(half_dt, acc.y, w.y);
           rb[4] = acc.x; rb[5] = acc.y;
         }
@@ -503,7 +509,7 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
         const int sidx = prm.tile_src_idx[q], se = prm.src_elem[sidx], sx = se % prm.mx, sy = se / prm.mx;
         const int a = X - sx * P, bb = Y - sy * P;
         if (a >= 0 && a <= P && bb >= 0 && bb <= P) {
-          const float val = (float)prm.stf[sidx];
+          const float val = (float)stp.stf[sidx];
           const float *sv = prm.src_vals + (size_t)sidx * 2 * NPE + 2 * (a + bb * N1);
           f[h][0] = fmaf(val, sv[0], f[h][0]); f[h][1] = fmaf(val, sv[1], f[h][1]);
         }
@@ -528,7 +534,7 @@ __device__ __forceinline__ bool tile_body(const Params &prm, int tx, int ty, con
           const int r = prm.tile_rec_idx[q], re = prm.rec_elem[r], rx = re % prm.mx, ry = re / prm.mx;
           const int a = X - rx * P, bb = Y - ry * P;
           if (a >= 0 && a <= P && bb >= 0 && bb <= P) {
-            float *rb = prm.rbuf_out + ((size_t)r * NPE + a + bb * N1) * 6;
+            float *rb = stp.rbuf_out + ((size_t)r * NPE + a + bb * N1) * 6;
             rb[0] = ux; rb[1] = uy; rb[2] = fmaf(half_dt, ax, wx); rb[3] = fmaf(half_dt, ay, wy);
             rb[4] = ax; rb[5] = ay;
           }
@@ -638,7 +644,7 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
           issue_region<P, TE, KAHAN>(txn, tyn, s ? stage0 : stage1, s ? bar0 : bar1, &tm_u, &tm_cu);
       }
     }
-    if (!tile_body<P, TE, NT, KAHAN, NOB == 1>(prm, tx, ty, s ? stage1 : stage0, bar, parity, ob, bo0, par_o, X1, X2,
+    if (!tile_body<P, TE, NT, KAHAN, NOB == 1>(prm, StepPtrs{prm.stf, prm.rbuf_out, prm.a_out}, tx, ty, s ? stage1 : stage0, bar, parity, ob, bo0, par_o, X1, X2,
                                                item, el, j, ecx, ecy, wj)) {
       if (threadIdx.x == 0) {
         atomicExch(prm.err, 1);
@@ -667,30 +673,16 @@ __device__ __forceinline__ const float *batch_rbuf(const Params &sh, int kblk)
   return (kblk & 1) ? sh.rbuf_in : sh.rbuf_out;
 }
 
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-
-// one warp copies a shot's parameters (16-byte pieces, one per lane) into shared memory, asynchronously
-__device__ __forceinline__ void copy_params_async(Params *dst, const Params *src)
-{
-  const int lane = threadIdx.x & 31;
-  if (lane < (int)(sizeof(Params) / 16))
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(reinterpret_cast<unsigned char *>(dst) + 16 * lane)),
-                 "l"(reinterpret_cast<const unsigned char *>(src) + 16 * lane)
-                 : "memory");
-  asm volatile("cp.async.commit_group;" ::: "memory");
-}
-
 template <int P, int TE, int NT, bool KAHAN, int NOB = owned_buffers(P),
-          int MINB = min_blocks(Layout<P, TE, KAHAN, NOB>::BATCH_TOTAL)>
+          int MINB = min_blocks(Layout<P, TE, KAHAN, NOB>::TOTAL)>
 __global__ void __launch_bounds__(NT, MINB)
-persist_batch(const BatchArgs ba)
+persist_batch(const __grid_constant__ BatchArgs ba)
 {
   typedef Geo<P, TE> G;
   typedef Layout<P, TE, KAHAN, NOB> L;
   constexpr int N1 = G::N1, NEX = G::NEX;
   static_assert(NT >= G::ITEMS, "one (element, line) item per thread");
   static_assert(NOB == 1 || NOB == 2, "one or two owned-box buffers");
-  static_assert(sizeof(Params) % 16 == 0 && sizeof(Params) / 16 <= 32, "Params copied in 16-byte pieces by one warp");
   const float *W = c_w[P - 1];
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char *stage0 = smem;
@@ -701,9 +693,6 @@ persist_batch(const BatchArgs ba)
   float2 *X2 = reinterpret_cast<float2 *>(smem + 2 * L::STAGE + NOB * L::OWNB + L::XCH);
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * L::STAGE + NOB * L::OWNB + 2 * L::XCH);
   const uint32_t bar0 = smem_u32(&bars[0]), bar1 = smem_u32(&bars[1]), bo0 = smem_u32(&bars[2]);
-  // two slots for the shot parameters of the current and the next tile (this step's pointers patched in)
-  Params *slot0 = reinterpret_cast<Params *>(smem + L::TOTAL);
-  Params *slot1 = reinterpret_cast<Params *>(smem + L::TOTAL + sizeof(Params));
 
   if (threadIdx.x == 0) {
     mbar_init(bar0, 1);
@@ -724,62 +713,50 @@ persist_batch(const BatchArgs ba)
   const int ecy = el / NEX, ecx = el - (el / NEX) * NEX;
   const float wj = (item < G::ITEMS) ? W[j] : 0.f;
 
-  // Per-tile pipeline.  Every thread keeps the work items of this tile and the next
-  // in registers (the list entry two tiles ahead is loaded one tile early).  The
-  // next tile's shot parameters are copied into the other parameter slot with
-  // cp.async by warp 0 while this tile is computed; its region copies and this tile's
-  // owned copies are issued at the top of this tile, so no dependent global load sits
-  // between two tiles.
+  // The shots' parameters are a kernel parameter (constant bank), so a tile reads
+  // its shot's directly.  Every thread keeps the work items of this tile and the
+  // next in registers (the list entry two tiles ahead is loaded one tile early);
+  // thread 0 issues the next tile's copies at the top of this tile, as in the
+  // single-shot kernel.
   const int stride = gridDim.x;
   int w = blockIdx.x;
   int2 cur = make_int2(0, 0), nxt = make_int2(0, 0);
   if (w < ba.nitems) cur = ba.items[w];
   if (w + stride < ba.nitems) nxt = ba.items[w + stride];
-  if (w < ba.nitems) {
-    if (threadIdx.x == 0) {
-      const CUtensorMap *m = ba.maps + 4 * cur.x;
-      if (NOB == 2) issue_both<P, TE, KAHAN>(cur.y & 0xFFFF, cur.y >> 16, stage0, ob0, bar0, m, m + 1, m + 2, m + 3);
-      else issue_region<P, TE, KAHAN>(cur.y & 0xFFFF, cur.y >> 16, stage0, bar0, m, m + 1);
-    }
-    if (threadIdx.x < 32) copy_params_async(slot0, ba.shots + cur.x);
+  if (w < ba.nitems && threadIdx.x == 0) {
+    const CUtensorMap *m = ba.maps + 4 * cur.x;
+    if (NOB == 2) issue_both<P, TE, KAHAN>(cur.y & 0xFFFF, cur.y >> 16, stage0, ob0, bar0, m, m + 1, m + 2, m + 3);
+    else issue_region<P, TE, KAHAN>(cur.y & 0xFFFF, cur.y >> 16, stage0, bar0, m, m + 1);
   }
   for (int it = 0; w < ba.nitems; it++, w += stride) {
     const int s = it & 1;
     const uint32_t bar = s ? bar1 : bar0;
     const uint32_t parity = (it >> 1) & 1;
     const int wn = w + stride;
-    Params &sp = s ? *slot1 : *slot0;
     unsigned char *ob = (NOB == 2 && s) ? ob1 : ob0;
     const uint32_t par_o = (uint32_t)(it & 1);   // the owned barrier (one owned buffer)
     const int2 nn = (wn + stride < ba.nitems) ? ba.items[wn + stride] : make_int2(0, 0);   // for the next tile
-    if (threadIdx.x < 32) {
-      cp_async_wait_all();
-      __syncwarp();
-      if (threadIdx.x == 0) {
-        // this step's pointers of the tile's shot
-        sp.stf = sp.stf + (size_t)ba.kblk * sp.nsrc;
-        sp.rbuf_out = const_cast<float *>(batch_rbuf(sp, ba.kblk));
-        if (!ba.write_a) sp.a_out = nullptr;
-        fence_proxy_async();
-        if (NOB == 1) {
-          const CUtensorMap *mc = ba.maps + 4 * cur.x;
-          issue_owned<P, TE, KAHAN>(cur.y & 0xFFFF, cur.y >> 16, ob0, bo0, mc + 2, mc + 3);
-        }
-        if (wn < ba.nitems) {
-          const CUtensorMap *m = ba.maps + 4 * nxt.x;
-          if (NOB == 2)
-            issue_both<P, TE, KAHAN>(nxt.y & 0xFFFF, nxt.y >> 16, s ? stage0 : stage1, s ? ob0 : ob1, s ? bar0 : bar1, m,
-                                     m + 1, m + 2, m + 3);
-          else
-            issue_region<P, TE, KAHAN>(nxt.y & 0xFFFF, nxt.y >> 16, s ? stage0 : stage1, s ? bar0 : bar1, m, m + 1);
-        }
+    if (threadIdx.x == 0) {
+      fence_proxy_async();
+      if (NOB == 1) {
+        const CUtensorMap *mc = ba.maps + 4 * cur.x;
+        issue_owned<P, TE, KAHAN>(cur.y & 0xFFFF, cur.y >> 16, ob0, bo0, mc + 2, mc + 3);
+      }
+      if (wn < ba.nitems) {
+        const CUtensorMap *m = ba.maps + 4 * nxt.x;
+        if (NOB == 2)
+          issue_both<P, TE, KAHAN>(nxt.y & 0xFFFF, nxt.y >> 16, s ? stage0 : stage1, s ? ob0 : ob1, s ? bar0 : bar1, m,
+                                   m + 1, m + 2, m + 3);
+        else
+          issue_region<P, TE, KAHAN>(nxt.y & 0xFFFF, nxt.y >> 16, s ? stage0 : stage1, s ? bar0 : bar1, m, m + 1);
       }
     }
-    __syncthreads();   // slot s is complete; every thread has left the previous tile, so the other slot is free
-    if (threadIdx.x < 32 && wn < ba.nitems) copy_params_async(s ? slot0 : slot1, ba.shots + nxt.x);
-    if (!tile_body<P, TE, NT, KAHAN, NOB == 1>(sp, cur.y & 0xFFFF, cur.y >> 16, s ? stage1 : stage0, bar, parity, ob,
-                                               bo0, par_o, X1, X2, item, el, j, ecx, ecy, wj)) {
-      if (threadIdx.x < 32) cp_async_wait_all();
+    // this step's pointers of the tile's shot
+    const Params &sp = ba.shots[cur.x];
+    const StepPtrs stp{sp.stf + (size_t)ba.kblk * sp.nsrc, const_cast<float *>(batch_rbuf(sp, ba.kblk)),
+                       ba.write_a ? sp.a_out : nullptr};
+    if (!tile_body<P, TE, NT, KAHAN, NOB == 1>(sp, stp, cur.y & 0xFFFF, cur.y >> 16, s ? stage1 : stage0, bar, parity,
+                                               ob, bo0, par_o, X1, X2, item, el, j, ecx, ecy, wj)) {
       if (threadIdx.x == 0) {
         atomicExch(ba.err, 1);
         mbar_wait_bounded(bar, parity);

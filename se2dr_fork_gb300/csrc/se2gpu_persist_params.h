@@ -35,17 +35,22 @@ struct Params {
   const int *tile_src_off, *tile_src_idx, *tile_rec_off, *tile_rec_idx;
 };
 
-// arguments of one batched step (many shots of one degree).  The shot table's
-// rbuf_out / rbuf_in are the shot's two receiver buffers (written at even / odd
-// steps of a block); stf and trace_row point at the shot's block staging.
+// shots per batched launch: their parameters travel in the kernel's parameter space
+// (constant bank), 96 x 288 B of the 32 KB a kernel parameter may take
+#define SE2P_BATCH_SHOTS 96
+
+// arguments of one batched step (up to SE2P_BATCH_SHOTS shots of one degree).  A
+// shot's rbuf_out / rbuf_in are its two receiver buffers (written at even / odd steps
+// of a block); stf and trace_row point at the shot's block staging.
 struct BatchArgs {
-  const Params *shots;         // per shot, for this step's input buffer
   const CUtensorMap *maps;     // [shot][4]: region u, region cu, owned w, owned cw of the input buffers
   const int2 *items;           // (shot, ty << 16 | tx) work list of tile coordinates
   int nshots, nitems;
   int kblk;                    // step index within the block
   int write_a;                 // store a_k (last step of a block)
   int *err;
+  Params shots[SE2P_BATCH_SHOTS];   // per shot, for this step's input buffer
 };
+static_assert(sizeof(BatchArgs) <= 32764, "a kernel parameter holds at most 32764 bytes");
 
 }  // namespace se2p

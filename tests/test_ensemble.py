@@ -133,3 +133,20 @@ def test_ensemble_errors():
         ens.set_tile_config(5, 0)
     with pytest.raises(G.GpuError, match="shot"):
         ens.fields(3)
+
+
+def test_group_larger_than_one_launch():
+    """A degree group of more shots than one launch carries (SE2P_BATCH_SHOTS = 96) runs as
+    several launches per step; shots in the first and the last launch stay bit-identical to
+    single-shot solvers."""
+    n = 100
+    setups = [H.Setup(S.shot(11, i, size=(3 + i % 5, 2 + i % 4), p=3, nt=24)) for i in range(n)]
+    ens = G.Ensemble(setups, "fp32_kahan", block=4)
+    got = ensemble_runs(ens, [9])
+    info = ens.info()
+    assert info["groups"] == 1 and info["launches"] == 2 * 9 + 3   # 2 launches per step + 3 receiver kernels
+    cfg = {3: ens.tile_config(3)}
+    for i in (0, 50, 95, 96, 99):
+        ref = single_runs([setups[i]], "fp32_kahan", [9], cfg)[0]
+        assert same(got[i], ref), i
+    ens.close()
