@@ -56,13 +56,13 @@ static const Entry *table(int *n)
   static Entry t[] = {
       entry<1, 15, 512>(), entry<1, 11, 288>(),
       entry<2, 10, 384>(), entry<2, 8, 256>(),
-      entry<3, 8, 352>(),  entry<3, 7, 256>(),
+      entry<3, 7, 256>(),  entry<3, 8, 352>(),
       // degree 4: 7x7 with one owned buffer kept at 2 CTAs per SM (92 registers) is the
       // fastest; sized for 3 CTAs it is capped at 64 registers and runs slower
       entry<4, 7, 320, 1, 2>(), entry<4, 7, 320, 2>(), entry<4, 6, 256, 2>(), entry<4, 8, 416>(),
       entry<5, 6, 320>(),  entry<5, 5, 224>(),
       entry<6, 5, 256>(),  entry<6, 4, 192>(),
-      entry<7, 5, 288>(),  entry<7, 4, 224>(),
+      entry<7, 4, 224>(),  entry<7, 5, 288>(),
       entry<8, 4, 256>(),  entry<8, 3, 160>(),
   };
   *n = (int)(sizeof(t) / sizeof(t[0]));
