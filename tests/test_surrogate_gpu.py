@@ -57,5 +57,5 @@ def test_solver_ladder_and_equal_misfit():
     assert coarse["nodes"] < mid["nodes"] < fine["nodes"]
     eq = SU.equal_misfit(lad, mid["misfit_mean"], 1.0)
     assert eq["solver"]["misfit_mean"] <= mid["misfit_mean"] and eq["gain"] == 1.0 / eq["solver"]["draws_per_s"]
-    assert eq["gain_solver_time"] >= eq["gain"]      # device time <= wall time
+    assert eq["gain_solver_time"] <= eq["gain"]      # the solver's device time is at most its wall time
     assert SU.equal_misfit(lad, -1.0, 1.0) == {"solver": None, "gain": None, "gain_solver_time": None}
