@@ -55,7 +55,7 @@ static const Entry *table(int *n)
 {
   static Entry t[] = {
       entry<1, 15, 512>(), entry<1, 11, 288>(),
-      entry<2, 10, 384>(), entry<2, 8, 256>(),
+      entry<2, 12, 512, 2, 2>(), entry<2, 10, 384>(), entry<2, 8, 256>(),
       entry<3, 7, 256>(),  entry<3, 8, 352>(),
       // degree 4: 7x7 with one owned buffer kept at 2 CTAs per SM (92 registers) is the
       // fastest; sized for 3 CTAs it is capped at 64 registers and runs slower
