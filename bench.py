@@ -161,6 +161,16 @@ def replica_seconds(local_seconds: float, dist=None, device=None) -> float:
     return float(t.item())
 
 
+def job_sum(x: float, dist=None, device: str = "cpu") -> float:
+    """Sum of a per-rank quantity over all ranks (the work of ranks that ran different shots)."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def replica_value(dof_per_replica: int, steps: int, world: int, seconds: float) -> float:
     """Whole-job DOF-updates/s of `world` replicas of the same workload (weak scaling)."""
     return world * dof_per_replica * steps / seconds
@@ -338,7 +348,7 @@ def run_sweep(args):
         del setup
 
 
-def run_ensemble(args):
+def run_ensemble(args, rank: int = 0, world: int = 1):
     """Batched ensemble: `--shots` seeded shots (mx, my ~ U{32..512}, p in {3,4,6}, 2 layers +
     elliptical inclusion, random source and moment tensor, Ricker f0 ~ U[5,20] Hz, 32 receivers,
     5000 steps each), FP32 with Kahan-compensated updates, one persistent launch per degree group
@@ -348,9 +358,14 @@ def run_ensemble(args):
     from se2dr_fork_gb300 import gpu as G
     from se2dr_fork_gb300 import host as H
     from se2dr_fork_gb300 import spec as S
-    torch.cuda.set_device(0)
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:   # one block of shots per GPU, no collective on the data path (timing only)
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     t0 = time.perf_counter()
-    specs = S.ensemble(args.shots, seed=3)
+    specs = S.ensemble_shard(args.shots, rank, seed=3)
     if args.ens_degree > 0:   # the same shots, all at one degree (per-degree efficiency of the batch kernel)
         specs = [sp.replace(p=args.ens_degree) for sp in specs]
     with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
@@ -395,40 +410,53 @@ def run_ensemble(args):
     ens.advance(args.block, traces=False)          # stage real STF values, build the graphs
     timed(args.warmup * args.block)
     launches0 = ens.info()["launches"]
-    with ClockSampler(0) as clk:
+    if dist:
+        dist.barrier()
+    with ClockSampler(local) as clk:
         secs = timed(args.steps)
     launches = ens.info()["launches"] - launches0
+    secs = replica_seconds(secs, dist, "cuda")
+    dof_job = job_sum(dof, dist, "cuda")
     per = secs / args.steps
     achieved = b * nodes / per / 1e9
     # end to end through the C-ABI: host STF upload per block, receiver rows back to host memory
     torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
     t0 = time.perf_counter()
     trs = ens.advance(args.steps)
-    e2e_s = time.perf_counter() - t0
+    e2e_s = replica_seconds(time.perf_counter() - t0, dist, "cuda")
     nrec_total = sum(su.nrec for su in setups)
     nsrc_total = sum(su.nsrc for su in setups)
     steps_per_shot = 5000
-    line = {"metric": METRIC, "value": dof * args.steps / secs, "unit": "DOF/s", "n_gpus": 1, "steps": args.steps,
+    if rank != 0:
+        ens.close()
+        dist.destroy_process_group()
+        return
+    line = {"metric": METRIC, "value": dof_job * args.steps / secs, "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup * args.block, "ms_per_step": 1e3 * per, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"ensemble: {args.shots} shots, mx, my ~ U{{32..512}}, p in {{3,4,6}}, 2 layers + "
                                    f"elliptical inclusion, random moment tensor, Ricker f0 ~ U[5,20] Hz, 32 receivers",
                        "precision": prec, "nodes": nodes, "dof": dof, "block": args.block,
+                       "parallelism": f"shot shards x{world} ({args.shots} shots per GPU)",
                        "degrees": {str(p): sum(1 for su in setups if su.p == p) for p in ens.degrees()},
                        "tile_configs": {str(p): ens.tile_config(p) for p in ens.degrees()},
                        "l2": "inputs larger than L2 (state %.1f GB)" % (nodes * 8 * (4 if prec == "fp32_kahan" else 2) / 1e9)},
-            "shots_per_s": args.shots * (args.steps / secs) / steps_per_shot,
+            "shots_per_s": world * args.shots * (args.steps / secs) / steps_per_shot,
             "shot_steps": steps_per_shot,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "traffic": None, "alg_bytes_per_node": b, "peak_kind": peak_kind},
             "clocks": clk.summary(), "gpu_launches": launches, "autotune": tuned or None,
-            "e2e": {"value": dof * args.steps / e2e_s, "unit": "DOF/s", "seconds": e2e_s,
-                    "shots_per_s": args.shots * (args.steps / e2e_s) / steps_per_shot,
+            "e2e": {"value": dof_job * args.steps / e2e_s, "unit": "DOF/s", "seconds": e2e_s,
+                    "shots_per_s": world * args.shots * (args.steps / e2e_s) / steps_per_shot,
                     "h2d_bytes_per_step": 8 * nsrc_total, "d2h_bytes_per_step": 8 * 7 * nrec_total,
                     "includes": "se2gpu_ensemble_advance: host STF upload per block, receiver rows to host memory"},
             "setup_seconds": {"host": t_setup, "ensemble_create": t_create},
             "trace_rows": int(sum(t.shape[0] for t in trs))}
     ens.close()
+    if dist:
+        dist.destroy_process_group()
     print(json.dumps(line), flush=True)
 
 
@@ -595,7 +623,7 @@ def main():
     if args.sweep:
         run_sweep(args)
     elif args.ensemble and args.impl == "ours":
-        run_ensemble(args)
+        run_ensemble(args, rank, world)
     elif args.surrogate and args.impl == "ours":
         run_surrogate(args)
     elif args.nn_step and args.impl == "ours":

@@ -195,6 +195,14 @@ def shot(seed: int, index: int, kind: int = 0, nt: Optional[int] = None, p: Opti
                 sources=[src], receivers=rec)
 
 
-def ensemble(nshots: int = 256, seed: int = 3, kind: int = 0, nt: Optional[int] = None) -> List[Spec]:
-    """The batched-ensemble workload: `nshots` seeded draws (256 shots, 5000 steps by default)."""
-    return [shot(seed, i, kind, nt) for i in range(nshots)]
+def ensemble(nshots: int = 256, seed: int = 3, kind: int = 0, nt: Optional[int] = None, first: int = 0) -> List[Spec]:
+    """The batched-ensemble workload: `nshots` seeded draws first, first + 1, ... (256 shots,
+    5000 steps by default)."""
+    return [shot(seed, i, kind, nt) for i in range(first, first + nshots)]
+
+
+def ensemble_shard(nshots: int, rank: int, seed: int = 3, kind: int = 0, nt: Optional[int] = None) -> List[Spec]:
+    """Rank `rank`'s shots of a multi-GPU ensemble: draws rank * nshots ... (rank + 1) * nshots - 1.
+    Shots are independent, so every GPU runs its own block of draws with no exchange (weak
+    scaling: the work per GPU is fixed)."""
+    return ensemble(nshots, seed, kind, nt, first=rank * nshots)
