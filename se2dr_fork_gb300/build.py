@@ -86,7 +86,7 @@ def _build_cuda_lib(name: str, units, deps, force: bool) -> str:
         with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
             list(ex.map(_run, jobs))
     if force or jobs or _newer(out, objs):
-        _run([NVCC, *ARCH, "-shared", "-o", out, *objs, "-lcudart"])
+        _run([NVCC, *ARCH, "-shared", "-o", out, *objs, "-lcudart", "-lpthread"])
     return out
 
 

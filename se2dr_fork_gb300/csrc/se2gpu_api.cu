@@ -17,6 +17,10 @@
 #include <cstdlib>
 #include <cstring>
 #include <algorithm>
+#include <atomic>
+#include <climits>
+#include <memory>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -73,6 +77,36 @@ static int dzero(se2gpu_solver *h, void **p, size_t bytes)
 }
 
 // upload an FP64 host array in the handle's compute precision
+// fn(begin, end) over [0, n) on up to 16 host threads (at least 1M items each): the
+// per-node host passes of se2gpu_create over meshes of tens of millions of nodes
+template <class F>
+static void host_parallel(long n, F fn)
+{
+  const long minchunk = 1L << 20;
+  long nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  nt = std::min(nt, (n + minchunk - 1) / minchunk);
+  if (nt <= 1) {
+    fn(0L, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (long t = 0; t < nt; t++) th.emplace_back(fn, n * t / nt, n * (t + 1) / nt);
+  for (std::thread &x : th) x.join();
+}
+
+// 1/M in the padded FP32 layout (padding nodes 0) straight from the caller's FP64 mass,
+// for devices that read pageable host memory (cudaDevAttrPageableMemoryAccess).  Double
+// division and the conversion to float round as on the host, so the values are the same.
+__global__ void k_minv_from_host(const double *__restrict__ mass, long nx_g, long ny_g, int pitch,
+                                 float *__restrict__ minv)
+{
+  const long np = ny_g * (long)pitch;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < np; i += (long)gridDim.x * blockDim.x) {
+    const long y = i / pitch, x = i - y * pitch;
+    minv[i] = (x < nx_g) ? __double2float_rn(1.0 / mass[y * nx_g + x]) : 0.f;
+  }
+}
+
 static int upload(se2gpu_solver *h, void **dst, const double *src, size_t n)
 {
   int rc = dalloc(h, dst, n * h->tsize);
@@ -239,8 +273,18 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
     const long node = ((long)(e % P->mx) * P->p + g % n1) + ((long)(e / P->mx) * P->p + g / n1) * nx_g;
     if (node != P->rec_node[r]) return fail(nullptr, SE2GPU_ERR_ARG, "receiver %d: node %d is not GLL point %d of element %d", r, P->rec_node[r], g, e);
   }
-  for (long i = 0; i < nnodes; i++)
-    if (!(P->mass[i] > 0.0) || !std::isfinite(P->mass[i])) return fail(nullptr, SE2GPU_ERR_ARG, "mass at node %ld is not positive", i);
+  {
+    std::atomic<long> bad(LONG_MAX);   // the first node whose mass is not positive and finite
+    host_parallel(nnodes, [&](long i0, long i1) {
+      for (long i = i0; i < i1; i++)
+        if (!(P->mass[i] > 0.0) || !std::isfinite(P->mass[i])) {
+          long cur = bad.load();
+          while (i < cur && !bad.compare_exchange_weak(cur, i)) {}
+          break;
+        }
+    });
+    if (bad.load() != LONG_MAX) return fail(nullptr, SE2GPU_ERR_ARG, "mass at node %ld is not positive", bad.load());
+  }
 
   se2gpu_solver *h = (se2gpu_solver *)calloc(1, sizeof(se2gpu_solver));
   h->mx = P->mx; h->my = P->my; h->p = P->p; h->n1 = n1; h->npe = npe;
@@ -302,12 +346,33 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
       TRY(dzero(h, (void **)&h->rbuf[b], (size_t)P->nrec * npe * 6 * 4));
     }
     TRY(dzero(h, (void **)&h->pa, np * 8));
-    {
-      std::vector<float> minv(np, 0.f);
-      for (long y = 0; y < ny_g; y++)
-        for (long x = 0; x < nx_g; x++) minv[(size_t)(y * h->pitch + x)] = (float)(1.0 / P->mass[y * nx_g + x]);
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, h->device) != cudaSuccess) {
+      cudaGetLastError();
+      pageable = 0;
+    }
+    if (pageable) {
+      // the device reads the mass where it lies (no staging copy of the whole array)
       TRY(dalloc(h, (void **)&h->pminv, np * 4));
-      if (cudaMemcpy(h->pminv, minv.data(), np * 4, cudaMemcpyHostToDevice) != cudaSuccess) { fail(h, SE2GPU_ERR_CUDA, "upload 1/M"); TRY(SE2GPU_ERR_CUDA); }
+      k_minv_from_host<<<4 * h->nsm, 256, 0, h->stream>>>(P->mass, nx_g, ny_g, h->pitch, h->pminv);
+      if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(h->stream) != cudaSuccess) {
+        fail(h, SE2GPU_ERR_CUDA, "1/M from host memory");
+        TRY(SE2GPU_ERR_CUDA);
+      }
+    } else {
+      // 1/M in the padded FP32 layout (padding nodes 0), row blocks on the host threads
+      std::unique_ptr<float[]> minv(new float[np]);
+      const int pitch = h->pitch;
+      host_parallel(ny_g, [&](long y0, long y1) {
+        for (long y = y0; y < y1; y++) {
+          float *row = minv.get() + (size_t)y * pitch;
+          const double *m = P->mass + y * nx_g;
+          for (long x = 0; x < nx_g; x++) row[x] = (float)(1.0 / m[x]);
+          for (long x = nx_g; x < pitch; x++) row[x] = 0.f;
+        }
+      });
+      TRY(dalloc(h, (void **)&h->pminv, np * 4));
+      if (cudaMemcpy(h->pminv, minv.get(), np * 4, cudaMemcpyHostToDevice) != cudaSuccess) { fail(h, SE2GPU_ERR_CUDA, "upload 1/M"); TRY(SE2GPU_ERR_CUDA); }
     }
     {
       cudaError_t e = se2p::set_tables(P->p, P->D, P->w1d);
