@@ -44,12 +44,12 @@ def test_host_library_exports():
 
 
 def test_gpu_library_is_sm103a(gpu_lib):
-    """The library carries sm_103a device code and is the one in the tree."""
-    from se2dr_fork_gb300 import gpu
+    """The library in use is the one built in the tree, for sm_103a only."""
+    from se2dr_fork_gb300 import build, gpu
     path = gpu.lib_path()
     assert path.startswith(os.path.join(ROOT, "se2dr_fork_gb300"))
-    blob = open(path, "rb").read()
-    assert b"sm_103a" in blob
+    assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+    assert all(a in build.NVCC_FLAGS for a in build.ARCH)
 
 
 def test_create_rejects_bad_problem_without_gpu(gpu_lib):
@@ -64,3 +64,56 @@ def test_create_rejects_bad_problem_without_gpu(gpu_lib):
     assert gpu.lib().se2gpu_create(ctypes.byref(pr), 64, 0, ctypes.byref(h)) == -1
     pr = gpu._CProblem(mx=4, my=4, p=2, dt=1e-3)
     assert gpu.lib().se2gpu_create(ctypes.byref(pr), 16, 0, ctypes.byref(h)) == -1
+
+
+def _small_problem():
+    from se2dr_fork_gb300 import gpu, host, spec
+    su = host.Setup(spec.demo(4, 3, p=2, tmax=1.0).replace(nt=4))
+    pr, keep = gpu._problem(su)
+    return su, pr, keep
+
+
+@pytest.mark.parametrize("case", ["too_large", "bad_receiver", "bad_mass", "bad_source", "negative_capacity",
+                                  "zero_dt", "missing_table"])
+def test_create_validates_the_problem_without_gpu(gpu_lib, case):
+    """Every argument check of se2gpu_create runs on the host before any device call."""
+    import numpy as np
+    from se2dr_fork_gb300 import gpu
+    su, pr, keep = _small_problem()
+    cap = 4
+    if case == "too_large":            # more than 2^31 DOF: 32-bit node indices would overflow
+        pr.mx, pr.my, pr.p = 30000, 30000, 8
+        msg = b"too large"
+    elif case == "bad_receiver":       # a receiver node that is not the named GLL point of its element
+        rn = np.array(su.rec_node, dtype=np.int32)
+        rn[0] += 1
+        keep.append(rn)
+        pr.rec_node = rn.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        msg = b"is not GLL point"
+    elif case == "bad_mass":           # a non-positive lumped mass (the first one is reported)
+        m = np.array(su.mass)
+        m[7] = 0.0
+        m[9] = -1.0
+        keep.append(m)
+        pr.mass = m.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        msg = b"node 7 is not positive"
+    elif case == "bad_source":
+        se = np.array(su.src_elem, dtype=np.int32)
+        se[0] = su.mx * su.my
+        keep.append(se)
+        pr.src_elem = se.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        msg = b"out of range"
+    elif case == "negative_capacity":
+        cap = -1
+        msg = b"negative"
+    elif case == "zero_dt":
+        pr.dt = 0.0
+        msg = b"time step"
+    else:
+        pr.mass = None
+        msg = b"missing problem table"
+    h = ctypes.c_void_p()
+    for precision in (64, 33, 32):
+        rc = gpu.lib().se2gpu_create(ctypes.byref(pr), precision, cap, ctypes.byref(h))
+        assert rc == -1 and not h.value, case
+        assert msg in gpu.lib().se2gpu_create_error(), gpu.lib().se2gpu_create_error()

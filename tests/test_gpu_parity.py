@@ -265,6 +265,31 @@ def test_errors_are_reported():
     assert sol.traces().shape == (4, 22)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32_kahan", "fp32"])
+def test_no_sources_no_receivers_stays_at_rest(precision):
+    """Empty source and receiver lists: the state stays exactly zero, the trace rows are empty,
+    and zero or negative step counts through the C-ABI do nothing or are refused."""
+    import ctypes as C
+    sp = S.demo(5, 4, p=3, tmax=1.0).replace(nt=12, sources=[], receivers=[])
+    sol = G.Solver(H.Setup(sp), precision)
+    tr = sol.run()
+    assert tr.shape == (0, 1)
+    assert all(not np.any(f) for f in sol.fields())
+    assert np.array_equal(sol.norms(), np.zeros(6))
+    lib = G.lib()
+    assert lib.se2gpu_advance(sol._h, 0, None) == 0
+    assert lib.se2gpu_advance(sol._h, -1, None) == -1 and b"negative" in lib.se2gpu_last_error(sol._h)
+
+
+def test_sources_need_stf_values():
+    import ctypes as C
+    sol = G.Solver(H.Setup(S.demo(4, 4, p=2, tmax=1.0).replace(nt=4)), "fp32_kahan")
+    assert G.lib().se2gpu_advance(sol._h, 2, None) == -1
+    assert b"stf values required" in G.lib().se2gpu_last_error(sol._h)
+    sol.advance(2)                      # with the host's STF values it runs
+    assert sol.traces().shape == (2, 22)
+
+
 @pytest.mark.parametrize("precision", ["fp32_kahan", "fp32"])
 @pytest.mark.parametrize("p", [3, 4, 6])
 def test_fp32_tile_configs_agree(p, precision):
