@@ -21,6 +21,7 @@
 #include <climits>
 #include <memory>
 #include <thread>
+#include <unistd.h>
 #include <utility>
 #include <vector>
 
@@ -77,12 +78,11 @@ static int dzero(se2gpu_solver *h, void **p, size_t bytes)
 }
 
 // upload an FP64 host array in the handle's compute precision
-// fn(begin, end) over [0, n) on up to 16 host threads (at least 1M items each): the
-// per-node host passes of se2gpu_create over meshes of tens of millions of nodes
+// fn(begin, end) over [0, n) on up to 16 host threads (at least minchunk items each): the
+// per-node host passes over meshes of tens of millions of nodes
 template <class F>
-static void host_parallel(long n, F fn)
+static void host_parallel(long n, F fn, long minchunk = 1L << 20)
 {
-  const long minchunk = 1L << 20;
   long nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
   nt = std::min(nt, (n + minchunk - 1) / minchunk);
   if (nt <= 1) {
@@ -107,12 +107,100 @@ __global__ void k_minv_from_host(const double *__restrict__ mass, long nx_g, lon
   }
 }
 
+// Bulk transfers between the caller's host arrays and the device, done by kernels that
+// read or write the host memory directly when the device can (pageable access): no
+// staging copy of whole arrays through pageable memory, and the layout conversion runs
+// on the device.  The arithmetic repeats the host paths operation for operation
+// (explicit round-to-nearest, nothing fused), so both give the same values.
+__global__ void k_copy_f64(double *__restrict__ dst, const double *__restrict__ src, size_t n)
+{
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+// FP32 leapfrog state (padded rows) -> FP64 (u, v, a) in the reference's node order
+__global__ void k_fields_to_host(const float2 *__restrict__ U, const float2 *__restrict__ W,
+                                 const float2 *__restrict__ CU, const float2 *__restrict__ CW,
+                                 const float2 *__restrict__ A, long nx_g, long ny_g, int pitch, double dt,
+                                 double hdt, double *u, double *v, double *a)
+{
+  const long nn = nx_g * ny_g;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nn; i += (long)gridDim.x * blockDim.x) {
+    const long y = i / nx_g, x = i - y * nx_g, k = y * pitch + x;
+    const float2 w = W[k], uu = U[k], ac = A[k];
+    const float2 cw = CW ? CW[k] : make_float2(0.f, 0.f), cu = CU ? CU[k] : make_float2(0.f, 0.f);
+    const double w0 = __dsub_rn((double)w.x, (double)cw.x), w1 = __dsub_rn((double)w.y, (double)cw.y);
+    const double u0 = __dsub_rn((double)uu.x, (double)cu.x), u1 = __dsub_rn((double)uu.y, (double)cu.y);
+    if (u) { u[2 * i] = __dsub_rn(u0, __dmul_rn(dt, w0)); u[2 * i + 1] = __dsub_rn(u1, __dmul_rn(dt, w1)); }
+    if (v) { v[2 * i] = __dsub_rn(w0, __dmul_rn(hdt, (double)ac.x)); v[2 * i + 1] = __dsub_rn(w1, __dmul_rn(hdt, (double)ac.y)); }
+    if (a) { a[2 * i] = (double)ac.x; a[2 * i + 1] = (double)ac.y; }
+  }
+}
+
+// FP64 (u, v, a) -> FP32 leapfrog state with its Kahan terms (padding nodes 0)
+__global__ void k_fields_from_host(const double *u, const double *v, const double *a, long nx_g, long ny_g,
+                                   int pitch, double dt, double hdt, float2 *__restrict__ U, float2 *__restrict__ W,
+                                   float2 *__restrict__ CU, float2 *__restrict__ CW, float2 *__restrict__ A)
+{
+  const long np = ny_g * (long)pitch;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < np; k += (long)gridDim.x * blockDim.x) {
+    const long y = k / pitch, x = k - y * pitch;
+    float2 Wk = make_float2(0.f, 0.f), Uk = Wk, CWk = Wk, CUk = Wk, Ak = Wk;
+    if (x < nx_g) {
+      const long n = y * nx_g + x;
+      double wv[2], uv[2];
+      for (int c = 0; c < 2; c++) {
+        const double uu = u ? u[2 * n + c] : 0.0, vv = v ? v[2 * n + c] : 0.0, aa = a ? a[2 * n + c] : 0.0;
+        wv[c] = __dadd_rn(vv, __dmul_rn(hdt, aa));
+        uv[c] = __dadd_rn(uu, __dmul_rn(dt, wv[c]));
+      }
+      Wk = make_float2(__double2float_rn(wv[0]), __double2float_rn(wv[1]));
+      Uk = make_float2(__double2float_rn(uv[0]), __double2float_rn(uv[1]));
+      CWk = make_float2(__double2float_rn(__dsub_rn((double)Wk.x, wv[0])), __double2float_rn(__dsub_rn((double)Wk.y, wv[1])));
+      CUk = make_float2(__double2float_rn(__dsub_rn((double)Uk.x, uv[0])), __double2float_rn(__dsub_rn((double)Uk.y, uv[1])));
+      Ak = make_float2(a ? __double2float_rn(a[2 * n]) : 0.f, a ? __double2float_rn(a[2 * n + 1]) : 0.f);
+    }
+    U[k] = Uk; W[k] = Wk; A[k] = Ak;
+    if (CU) { CU[k] = CUk; CW[k] = CWk; }
+  }
+}
+
+// Output arrays the device is about to write: fault their pages in on the host threads
+// first (one store per page), since a first touch taken through the device is much
+// slower.  The stores write zeros into memory that is overwritten next.
+static void prefault_output(double *p, size_t n)
+{
+  if (!p || !n) return;
+  const long page = std::max(4096L, sysconf(_SC_PAGESIZE));
+  const size_t per = (size_t)page / sizeof(double);
+  const long npages = (long)((n + per - 1) / per);
+  host_parallel(npages, [&](long i0, long i1) {
+    volatile double *q = p;
+    for (long i = i0; i < i1; i++) q[(size_t)i * per] = 0.0;
+  }, 256);
+}
+
+// copy n doubles between host and device through a kernel (pageable access) or cudaMemcpy
+static int copy_f64(se2gpu_solver *h, double *dst, const double *src, size_t n, cudaMemcpyKind kind)
+{
+  if (!n) return 0;
+  if (h->pageable) {
+    if (kind == cudaMemcpyDeviceToHost) prefault_output(dst, n);
+    k_copy_f64<<<4 * h->nsm, 256, 0, h->stream>>>(dst, src, n);
+    CK(h, cudaGetLastError());
+    CK(h, cudaStreamSynchronize(h->stream));
+  } else {
+    CK(h, cudaMemcpy(dst, src, n * 8, kind));
+  }
+  return 0;
+}
+
 static int upload(se2gpu_solver *h, void **dst, const double *src, size_t n)
 {
   int rc = dalloc(h, dst, n * h->tsize);
   if (rc) return rc;
   if (h->tsize == 8) {
-    CK(h, cudaMemcpy(*dst, src, n * 8, cudaMemcpyHostToDevice));
+    return copy_f64(h, (double *)*dst, src, n, cudaMemcpyHostToDevice);
   } else {
     std::vector<float> tmp(n);
     for (size_t i = 0; i < n; i++) tmp[i] = (float)src[i];
@@ -162,6 +250,16 @@ extern "C" void se2gpu_destroy(se2gpu_solver *h)
 static int upload_leapfrog(se2gpu_solver *h, const double *u, const double *v, const double *a)
 {
   const size_t np = (size_t)h->ny_g * h->pitch;
+  if (h->pageable) {
+    const int c = h->cur;
+    const bool kahan = is_kahan(h);
+    k_fields_from_host<<<4 * h->nsm, 256, 0, h->stream>>>(u, v, a, h->nx_g, h->ny_g, h->pitch, h->dt, 0.5 * h->dt,
+                                                          h->pu[c], h->pw[c], kahan ? h->pcu[c] : nullptr,
+                                                          kahan ? h->pcw[c] : nullptr, h->pa);
+    CK(h, cudaGetLastError());
+    CK(h, cudaStreamSynchronize(h->stream));
+    return 0;
+  }
   std::vector<float2> U(np), W(np), CU(np), CW(np), A(np);
   const double dt = h->dt, hdt = 0.5 * h->dt;
   for (long y = 0; y < h->ny_g; y++)
@@ -300,6 +398,10 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
 #define TRY(x) do { if ((rc = (x)) != 0) { snprintf(g_create_err, sizeof(g_create_err), "%s", h->err); se2gpu_destroy(h); return rc; } } while (0)
   if (cudaGetDevice(&h->device) != cudaSuccess) { cudaGetLastError(); free(h); return fail(nullptr, SE2GPU_ERR_CUDA, "no CUDA device"); }
   cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->device);
+  if (cudaDeviceGetAttribute(&h->pageable, cudaDevAttrPageableMemoryAccess, h->device) != cudaSuccess) {
+    cudaGetLastError();
+    h->pageable = 0;
+  }
   {
     cudaError_t e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { free(h); return fail(nullptr, SE2GPU_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e)); }
@@ -346,12 +448,7 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
       TRY(dzero(h, (void **)&h->rbuf[b], (size_t)P->nrec * npe * 6 * 4));
     }
     TRY(dzero(h, (void **)&h->pa, np * 8));
-    int pageable = 0;
-    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, h->device) != cudaSuccess) {
-      cudaGetLastError();
-      pageable = 0;
-    }
-    if (pageable) {
+    if (h->pageable) {
       // the device reads the mass where it lies (no staging copy of the whole array)
       TRY(dalloc(h, (void **)&h->pminv, np * 4));
       k_minv_from_host<<<4 * h->nsm, 256, 0, h->stream>>>(P->mass, nx_g, ny_g, h->pitch, h->pminv);
@@ -583,7 +680,7 @@ extern "C" int se2gpu_set_fields(se2gpu_solver *h, const double *u, const double
   if (is_f64(h)) {
     const double *src[3] = {u, v, a};
     for (int f = 0; f < 3; f++)
-      if (src[f]) CK(h, cudaMemcpy(h->f64[h->cur][f], src[f], n * 8, cudaMemcpyHostToDevice));
+      if (src[f] && (rc = copy_f64(h, (double *)h->f64[h->cur][f], src[f], n, cudaMemcpyHostToDevice))) return rc;
     return 0;
   }
   // FP32: unspecified fields keep their current values
@@ -606,7 +703,20 @@ extern "C" int se2gpu_get_fields(se2gpu_solver *h, double *u, double *v, double 
   if (is_f64(h)) {
     double *dst[3] = {u, v, a};
     for (int f = 0; f < 3; f++)
-      if (dst[f]) CK(h, cudaMemcpy(dst[f], h->f64[h->cur][f], n * 8, cudaMemcpyDeviceToHost));
+      if (dst[f] && (rc = copy_f64(h, dst[f], (const double *)h->f64[h->cur][f], n, cudaMemcpyDeviceToHost))) return rc;
+    return 0;
+  }
+  if (h->pageable) {
+    const int c = h->cur;
+    const bool kahan = is_kahan(h);
+    prefault_output(u, n);
+    prefault_output(v, n);
+    prefault_output(a, n);
+    k_fields_to_host<<<4 * h->nsm, 256, 0, h->stream>>>(h->pu[c], h->pw[c], kahan ? h->pcu[c] : nullptr,
+                                                        kahan ? h->pcw[c] : nullptr, h->pa, h->nx_g, h->ny_g, h->pitch,
+                                                        h->dt, 0.5 * h->dt, u, v, a);
+    CK(h, cudaGetLastError());
+    CK(h, cudaStreamSynchronize(h->stream));
     return 0;
   }
   const size_t np = (size_t)h->ny_g * h->pitch;

@@ -11,6 +11,7 @@
 #include "se2gpu_persist_params.h"
 
 struct se2gpu_solver {
+  int pageable;      // the device reads and writes pageable host memory (cudaDevAttrPageableMemoryAccess)
   int mx, my, p, n1, npe, nx_g, ny_g, precision;
   long nnodes;
   int nsrc, nrec, trace_cap, rows_written;
