@@ -229,8 +229,20 @@ step_kernel(const StepParams<T> prm)
   __syncthreads();
 
   // ---- phase 2: stress at every GLL point of tile + halo -------------
-  for (int idx = threadIdx.x; idx < NEX * NEY * NPE; idx += blockDim.x) {
-    const int el = idx / NPE, q = idx - el * NPE;
+  // FP64 walks the points row by row of their element (qj outermost), so the
+  // shear-strain sum's branch on qj is the same for nearly every thread of a warp
+  const int NEL = NEX * NEY;
+  for (int it = threadIdx.x; it < NEL * NPE; it += blockDim.x) {
+    int el, q;
+    if constexpr (F64) {
+      const int qj_ = it / (NEL * N1), r = it - qj_ * (NEL * N1);
+      el = r / N1;
+      q = (r - el * N1) + qj_ * N1;
+    } else {
+      el = it / NPE;
+      q = it - el * NPE;
+    }
+    const int idx = el * NPE + q;
     const int ecy = el / NEX, ecx = el - ecy * NEX;
     const int qj = q / N1, qi = q - qj * N1;
     const int ex = EX0 + ecx, ey = EY0 + ecy;
@@ -287,8 +299,34 @@ step_kernel(const StepParams<T> prm)
   __syncthreads();
 
   // ---- phase 3: divergence, ordered element sum, source, update -------
+  // FP64 takes the nodes on element-column lines (2 elements along x) first and the
+  // others after, each group ordered by the node's row within its element (which
+  // decides the branches of the element sums) and then by row and column, so a warp's
+  // threads loop over the same elements and take the same branches
+  const int NC1 = (OW + P - 1) / P, NC0 = OW - NC1;   // columns on / between element lines
   for (int o = threadIdx.x; o < OW * OH; o += blockDim.x) {
-    const int oy = o / OW, ox = o - oy * OW;
+    int oy, ox;
+    if constexpr (F64) {
+      const bool on = o < NC1 * OH;
+      const int nc = on ? NC1 : NC0;
+      int r = on ? o : o - NC1 * OH, b = 0;
+      for (; b < P - 1; b++) {          // rows oy = b, b + P, ... of the tile
+        const int nb = nc * ((OH - b + P - 1) / P);
+        if (r < nb) break;
+        r -= nb;
+      }
+      const int row = r / nc, col = r - row * nc;
+      oy = row * P + b;
+      if (on) {
+        ox = col * P;
+      } else {
+        constexpr int PM = (P > 1) ? P - 1 : 1;   // interior nodes per element along x (degree 1: none)
+        ox = (col / PM) * P + (col % PM) + 1;
+      }
+    } else {
+      oy = o / OW;
+      ox = o - oy * OW;
+    }
     const int X = X0 + ox, Y = Y0 + oy;
     T fx = 0, fy = 0;
     const int eyA = (Y % P == 0) ? Y / P - 1 : Y / P, exA = (X % P == 0) ? X / P - 1 : X / P;
