@@ -74,7 +74,7 @@ template <int P> struct Tile { static constexpr int TE = (P == 1) ? 32 : (P == 2
 
 // shared-memory carve, identical on host and device
 struct Smem {
-  size_t U, V, CU, CV, S, Dx, Dy, W, D, total;
+  size_t U, V, CU, CV, S, Dx, Dy, W, D, Nf, total;
 };
 __host__ __device__ inline size_t se2_align16(size_t x) { return (x + 15) & ~size_t(15); }
 template <int P, typename T, bool KAHAN>
@@ -95,6 +95,11 @@ __host__ __device__ inline Smem smem_layout()
   s.Dy = o; o = se2_align16(o + sizeof(T) * (TE + 1) * NPE);
   s.W = o;  o = se2_align16(o + sizeof(T) * NPE);
   s.D = o;  o = se2_align16(o + sizeof(T) * NPE);
+  // FP64: -(detJ * w_q) per element and point, the factor of every divergence term, where
+  // the table still leaves room for 2 CTAs per SM (otherwise it is formed per term)
+  const size_t nf = (sizeof(T) == 8) ? sizeof(T) * NE * NPE : 0;
+  s.Nf = o;
+  if (nf && 2 * (se2_align16(o + nf) + 1024) <= 233472) o = se2_align16(o + nf);
   s.total = o;
   return s;
 }
@@ -162,6 +167,7 @@ step_kernel(const StepParams<T> prm)
   T *sDy = reinterpret_cast<T *>(smem_raw + L.Dy);
   T *sW = reinterpret_cast<T *>(smem_raw + L.W);
   T *sD = reinterpret_cast<T *>(smem_raw + L.D);
+  T *sNf = reinterpret_cast<T *>(smem_raw + L.Nf);
 
   const int ntiles = prm.ntx * prm.nty;
   if ((int)blockIdx.x >= ntiles) {
@@ -225,6 +231,12 @@ step_kernel(const StepParams<T> prm)
   if constexpr (F64) {
     for (int i = threadIdx.x; i < NEX * NPE; i += blockDim.x) sDx[i] = mul(prm.iJ00[EX0 + i / NPE], prm.D[i % NPE]);
     for (int i = threadIdx.x; i < NEY * NPE; i += blockDim.x) sDy[i] = mul(prm.iJ11[EY0 + i / NPE], prm.D[i % NPE]);
+    // the same value the divergence would form per term: -(J00 J11) * w_q, operand order kept
+    if (L.total > L.Nf)
+    for (int i = threadIdx.x; i < NEX * NEY * NPE; i += blockDim.x) {
+      const int el = i / NPE, q = i - el * NPE, ecy = el / NEX, ecx = el - ecy * NEX;
+      sNf[i] = -mul(mul(prm.J00[EX0 + ecx], prm.J11[EY0 + ecy]), prm.wq[q]);
+    }
   }
   __syncthreads();
 
@@ -339,7 +351,9 @@ step_kernel(const StepParams<T> prm)
         const int a = X - ex * P, b = Y - ey * P;
         const T *Sxx = sSxx + el * NPE, *Syy = sSyy + el * NPE, *Sxy = sSxy + el * NPE;
         if constexpr (F64) {
-          const double detJ = mul(prm.J00[ex], prm.J11[ey]);
+          const bool nft = L.total > L.Nf;   // the factor table exists (room for 2 CTAs)
+          const double *nfe = sNf + el * NPE;
+          const double detJ = nft ? 0.0 : mul(prm.J00[ex], prm.J11[ey]);
           const double *dx = sDx + ecx * NPE, *dy = sDy + ecy * NPE;
           double gx = 0.0, gy = 0.0;
           // quadrature points ascending: column below b, row b, column above b
@@ -347,7 +361,7 @@ step_kernel(const StepParams<T> prm)
           for (int qj = 0; qj < N1; qj++) {
             if (qj != b) {
               const int q = a + qj * N1;
-              const double nf = -mul(detJ, sW[q]);
+              const double nf = nft ? nfe[q] : -mul(detJ, sW[q]);
               const double dNy = dy[qj * N1 + b];
               gx = add(gx, mul(nf, mul(dNy, Sxy[q])));
               gy = add(gy, mul(nf, mul(dNy, Syy[q])));
@@ -355,7 +369,7 @@ step_kernel(const StepParams<T> prm)
 #pragma unroll
               for (int qi = 0; qi < N1; qi++) {
                 const int q = qi + b * N1;
-                const double nf = -mul(detJ, sW[q]);
+                const double nf = nft ? nfe[q] : -mul(detJ, sW[q]);
                 const double dNx = dx[qi * N1 + a];
                 double tx, ty;
                 if (qi == a) {
