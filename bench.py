@@ -112,9 +112,10 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(threads: int, rows: int, steps: int, warmup: int = 1):
+def cpu_baseline(threads: int, rows: int, steps: int, warmup: int = 1, record: bool = True):
     """The oracle port (the reference algorithm) on host threads: each thread an
-    independent solve of a 2048 x `rows` element strip of the workload."""
+    independent solve of a 2048 x `rows` element strip of the workload, with receiver
+    output (the reference's default) or without it (-ignore_receiver_output)."""
     from oracle import oracle as O
     from se2dr_fork_gb300 import spec as S
     from se2dr_fork_gb300 import host as H
@@ -123,11 +124,12 @@ def cpu_baseline(threads: int, rows: int, steps: int, warmup: int = 1):
     # same element shape as the full workload: the strip is rows/2048 of its height
     h = 20000.0 * rows / 2048.0
     sp = sp.replace(scale=(20000.0, h), shift=(-10000.0, -h / 2), receivers=[(x, 0.0) for x, _ in sp.receivers])
-    secs = O.bench(sp, threads, warmup, steps, record=True)
+    secs = O.bench(sp, threads, warmup, steps, record=record)
     dof = sp.ndof
+    rec = "receivers recorded" if record else "-ignore_receiver_output"
     return {"value": threads * dof * steps / secs, "seconds": secs, "dof_per_thread": dof,
             "sample": f"{threads} independent solves of a 2048x{rows}-element strip of the workload "
-                      f"(degree 4, {dof} DOF each, receivers recorded), {steps} steps after {warmup} warm-up"}
+                      f"(degree 4, {dof} DOF each, {rec}), {steps} steps after {warmup} warm-up"}
 
 
 def run_reference(args, rank, world):
@@ -287,6 +289,8 @@ def run_ours(args, rank, world):
         try:
             c1 = cpu_baseline(1, args.cpu_rows, max(2, args.cpu_steps // 2))
             cpu["single_core_value"] = c1["value"]
+            cn = cpu_baseline(threads, args.cpu_rows, args.cpu_steps, record=False)
+            cpu["no_receiver_output_value"] = cn["value"]
         except Exception:
             pass
     line = {"metric": METRIC, "value": head["value"], "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
