@@ -4,7 +4,6 @@ value -- runs here on CPU as two gloo ranks."""
 import os
 import socket
 
-import pytest
 import torch.multiprocessing as mp
 
 

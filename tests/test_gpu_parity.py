@@ -8,7 +8,7 @@ receiver traces (the tolerance the target states for FP32).
 import numpy as np
 import pytest
 
-from golden_util import FP32_COMPONENT_TOL, K_SHEAR, fp32_errors, fp32_errors_ok, load, rel_l2, spec_of
+from golden_util import FP32_COMPONENT_TOL, fp32_errors, fp32_errors_ok, load, rel_l2, spec_of
 from oracle import oracle as O
 from se2dr_fork_gb300 import gpu as G
 from se2dr_fork_gb300 import host as H
@@ -269,7 +269,6 @@ def test_errors_are_reported():
 def test_no_sources_no_receivers_stays_at_rest(precision):
     """Empty source and receiver lists: the state stays exactly zero, the trace rows are empty,
     and zero or negative step counts through the C-ABI do nothing or are refused."""
-    import ctypes as C
     sp = S.demo(5, 4, p=3, tmax=1.0).replace(nt=12, sources=[], receivers=[])
     sol = G.Solver(H.Setup(sp), precision)
     tr = sol.run()
@@ -282,7 +281,6 @@ def test_no_sources_no_receivers_stays_at_rest(precision):
 
 
 def test_sources_need_stf_values():
-    import ctypes as C
     sol = G.Solver(H.Setup(S.demo(4, 4, p=2, tmax=1.0).replace(nt=4)), "fp32_kahan")
     assert G.lib().se2gpu_advance(sol._h, 2, None) == -1
     assert b"stf values required" in G.lib().se2gpu_last_error(sol._h)
