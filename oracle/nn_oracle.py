@@ -1,5 +1,6 @@
 """FP64 CPU restatement of the surrogate network of include/se2nn.h -- TEST
-INFRASTRUCTURE ONLY (the checker of libse2nn.so; nothing in the product imports it).
+INFRASTRUCTURE ONLY (the oracle that libse2nn.so is tested against; nothing in the
+product imports it).
 
 The network has no counterpart in the reference (se2wave.c has no learned
 component): this restates, in numpy float64, exactly the architecture the

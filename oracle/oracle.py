@@ -2,8 +2,8 @@
 driver built in place (oracle/_ref/ref_driver).
 
 TEST INFRASTRUCTURE ONLY.  Only tests/, ``__graft_entry__.smoke()`` and the CPU
-baseline legs of bench.py use this module, and only as the checker or as the
-timed CPU implementation; the product package never imports it.
+baseline legs of bench.py use this module, and only as the values results are
+compared with or as the timed CPU implementation; the product package never imports it.
 """
 from __future__ import annotations
 
