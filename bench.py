@@ -491,12 +491,13 @@ def run_surrogate(args):
         nets.append(net)
         stats.append(st)
     fwd = SU.forward_flops(SU.net_config())
+    inf = SU.for_inference(nets, 128)   # the same networks, 128 draws per forward pass
     # inference throughput of the ensemble of networks, warm (a first call on a few draws
     # builds the streams and buffers), host-timed including the copy back
-    SU.predict(nets, dtest, np.arange(min(dtest.n, 64)))
+    SU.predict(inf, dtest, np.arange(min(dtest.n, 64)))
     torch.cuda.synchronize()
     tq = time.perf_counter()
-    preds = SU.predict(nets, dtest, np.arange(dtest.n))
+    preds = SU.predict(inf, dtest, np.arange(dtest.n))
     t_pred = time.perf_counter() - tq
     mean, dis = preds.mean(axis=0), SU.disagreement(preds)
     mis = SU.rel_l2(mean, test.traces)
@@ -507,7 +508,7 @@ def run_surrogate(args):
         what_if.append({"threshold": th, "fallback_rate": float(1 - acc.mean()),
                         "accepted_misfit_max": float(mis[acc].max()) if acc.any() else None,
                         "accepted_misfit_mean": float(mis[acc].mean()) if acc.any() else None})
-    served = SU.serve(nets, dtest, test.specs, threshold=args.threshold, audit=0.05)
+    served = SU.serve(inf, dtest, test.specs, threshold=args.threshold, audit=0.05)
     solver_sps = dtest.n / test.wall_seconds
     # the gain at equal misfit: coarser solvers on the in-distribution held-out draws
     ladder = SU.solver_ladder(te_in.specs, te_in.traces)

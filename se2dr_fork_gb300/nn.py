@@ -145,6 +145,7 @@ class Network:
     def set_receivers(self, rec_x):
         r = np.ascontiguousarray(rec_x, dtype=np.int32)
         self._check(lib().se2nn_set_receivers(self._h, r.ctypes.data_as(_ip)), "se2nn_set_receivers")
+        self.rec_x = r.copy()
 
     def forward(self, x, out):
         """out[b] (fp32 torch tensor [B, nrec, nout]) = network(x[b]) (bf16 torch tensor [B, ny, nx, cin])."""

@@ -280,11 +280,28 @@ def train(data: DeviceData, idx_train: np.ndarray, rec_x: np.ndarray, seed: int 
     return net, {"loss": hist, "samples_per_s": total * batch / secs, "seconds": secs, "steps": total}
 
 
-def predict(nets, data: DeviceData, idx: np.ndarray, batch: int = 32) -> np.ndarray:
-    """[K, n, 16, 2048] predictions (unscaled) of every network for draws idx.  The outputs
-    stay on the device until all batches are done, then come back in one copy."""
+def for_inference(nets, max_batch: int = 128, rec_x: Optional[np.ndarray] = None):
+    """Copies of trained networks whose activation buffers take `max_batch` draws per
+    forward pass (training runs 32): the small GEMMs of one pass are latency-bound, so
+    larger passes serve more draws per second.  Parameters and receivers are the same."""
+    out = []
+    for net in nets:
+        cfg = dataclasses.replace(net.cfg, max_batch=max_batch)
+        n2 = N.Network(cfg, seed=0)
+        n2.set_params(net.params())
+        n2.set_receivers(net.rec_x if rec_x is None else rec_x)
+        out.append(n2)
+    return out
+
+
+def predict(nets, data: DeviceData, idx: np.ndarray, batch: Optional[int] = None) -> np.ndarray:
+    """[K, n, 16, 2048] predictions (unscaled) of every network for draws idx, `batch` draws per
+    pass (default: what the networks' buffers take).  The outputs stay on the device until all
+    batches are done, then come back in one copy."""
     import torch
     K = len(nets)
+    if batch is None:
+        batch = min(net.cfg.max_batch for net in nets)
     stream = torch.cuda.Stream()
     for net in nets:
         net.set_stream(stream.cuda_stream)

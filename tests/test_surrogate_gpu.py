@@ -59,3 +59,20 @@ def test_solver_ladder_and_equal_misfit():
     assert eq["solver"]["misfit_mean"] <= mid["misfit_mean"] and eq["gain"] == 1.0 / eq["solver"]["draws_per_s"]
     assert eq["gain_solver_time"] <= eq["gain"]      # the solver's device time is at most its wall time
     assert SU.equal_misfit(lad, -1.0, 1.0) == {"solver": None, "gain": None, "gain_solver_time": None}
+
+
+def test_inference_copies_predict_the_same():
+    """Networks re-created for larger inference batches (for_inference) carry the same
+    parameters and give the same predictions as the trained ones, whatever the batch."""
+    specs = SU.specs_of(31, 6)
+    mats, src = SU.inputs_of(specs)
+    ds = SU.Dataset(mats, src, np.zeros((6, SU.NREC, 2 * SU.NSAMP), dtype=np.float32), np.zeros(6), specs=specs)
+    data = SU.DeviceData(ds, scale=1.0)
+    from se2dr_fork_gb300 import nn as N
+    net = N.Network(SU.net_config(4), seed=3)
+    net.set_receivers(SU.receiver_cells(specs[0]))
+    big = SU.for_inference([net], max_batch=8)
+    assert big[0].cfg.max_batch == 8 and np.array_equal(big[0].params(), net.params())
+    a = SU.predict([net], data, np.arange(6))            # passes of 4 + 2
+    b = SU.predict(big, data, np.arange(6))              # one pass of 6
+    assert np.array_equal(a, b)
