@@ -59,6 +59,24 @@ def alg_bytes_per_node(precision: str, ne: int, nnodes: int) -> float:
     return 2 * 2 * 8 + 4 + 8 * cell                # leapfrog u,w (float2) in+out, 1/M, (lambda, mu)
 
 
+def reference_bytes_per_node(precision: str, ne: int, nnodes: int) -> float:
+    """DRAM bytes per node per step of the reference's own update sequence (se2wave.c:4722-4775)
+    in this precision: u, v, a read and written (FP32+Kahan: also the compensation terms of u
+    and v), 1/M and the cell's (lambda, mu).  The kick-drift state above needs no a, so it moves
+    fewer bytes for the same DOF-updates; this count is the one to compare other
+    implementations of the reference's scheme against."""
+    words = {"fp64": 13, "fp32": 13, "fp32_kahan": 21}[precision]
+    wb = 8 if precision == "fp64" else 4
+    return (words + 2 * ne / nnodes) * wb
+
+
+def reference_formulation(precision: str, ne: int, nnodes: int, per_step: float, hbm: float) -> dict:
+    rb = reference_bytes_per_node(precision, ne, nnodes)
+    ach = rb * nnodes / per_step / 1e9
+    return {"bytes_per_node": rb, "achieved": ach, "frac": ach / hbm,
+            "note": "reference update sequence's bytes (u, v, a and Kahan terms of u, v) at the same step time"}
+
+
 class ClockSampler:
     """nvidia-smi clocks/throttle sampling during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -254,7 +272,8 @@ def run_ours(args, rank, world):
                                                   if prec in MEASURED_TRAFFIC_PER_NODE and args.mx == 2048
                                                   and args.degree == 4 else None),
                                       "traffic_note": "ncu DRAM bytes per node at 1024^2 x nodes (bytes per launch)",
-                                      "alg_bytes_per_node": b, "peak_kind": peak_kind}}
+                                      "alg_bytes_per_node": b, "peak_kind": peak_kind,
+                                      "reference_formulation": reference_formulation(prec, ne, nnodes, per, hbm)}}
 
     # end to end through the C-ABI: create (upload from host) + K steps + traces read back + destroy
     prec = args.precision
@@ -450,7 +469,8 @@ def run_ensemble(args, rank: int = 0, world: int = 1):
             "shots_per_s": world * args.shots * (args.steps / secs) / steps_per_shot,
             "shot_steps": steps_per_shot,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": None, "alg_bytes_per_node": b, "peak_kind": peak_kind},
+                         "traffic": None, "alg_bytes_per_node": b, "peak_kind": peak_kind,
+                         "reference_formulation": reference_formulation(prec, ne, nodes, per, hbm)},
             "clocks": clk.summary(), "gpu_launches": launches, "autotune": tuned or None,
             "e2e": {"value": dof_job * args.steps / e2e_s, "unit": "DOF/s", "seconds": e2e_s,
                     "shots_per_s": world * args.shots * (args.steps / e2e_s) / steps_per_shot,
