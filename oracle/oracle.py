@@ -187,10 +187,6 @@ def bench(spec, nthreads: int, warmup: int, nsteps: int, record: bool = True) ->
 # ---------------------------------------------------------------------------
 # the reference itself, compiled in place (only where the reference tree exists)
 # ---------------------------------------------------------------------------
-def ref_available() -> bool:
-    return os.path.exists(REF_DRIVER)
-
-
 def build_ref(refdir: str = "/root/reference") -> bool:
     if not os.path.exists(os.path.join(refdir, "se2wave.c")):
         return False
