@@ -78,6 +78,18 @@ const char *se2gpu_create_error(void);
 int se2gpu_set_stream(se2gpu_solver *h, void *stream);
 int se2gpu_synchronize(se2gpu_solver *h);
 
+/* Self-test of failure detection (no counterpart in the reference).  Every wait of
+   the FP32 step kernels on their tile copies is bounded: on expiry the kernel raises
+   the handle's error flag and returns, and the next call that checks the flag
+   fails with SE2GPU_ERR_CUDA.  This call runs that same bounded wait, with a limit
+   of 256 polls, on an mbarrier that nothing arrives at, on the handle's stream.  It
+   returns what se2gpu_synchronize would then return: SE2GPU_ERR_CUDA with the
+   bounded-wait message, or 0 if the flag was not raised.  *seconds (if not NULL)
+   receives the wait's duration on the device clock.  The flag stays raised, as
+   after a real expiry: destroy the handle afterwards.  No copy is in flight and
+   nothing faults, so the CUDA context and other handles stay usable. */
+int se2gpu_selftest_wait_expiry(se2gpu_solver *h, double *seconds);
+
 /* Fields as FP64 host arrays of 2*nnodes (any may be NULL). */
 int se2gpu_set_fields(se2gpu_solver *h, const double *u, const double *v, const double *a);
 int se2gpu_get_fields(se2gpu_solver *h, double *u, double *v, double *a);

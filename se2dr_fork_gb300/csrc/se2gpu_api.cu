@@ -507,6 +507,21 @@ extern "C" int se2gpu_synchronize(se2gpu_solver *h)
   return check_err_flag(h);
 }
 
+extern "C" int se2gpu_selftest_wait_expiry(se2gpu_solver *h, double *seconds)
+{
+  if (!h) return SE2GPU_ERR_ARG;
+  CK(h, cudaStreamSynchronize(h->stream));
+  unsigned long long *ns_dev = nullptr, ns = 0;
+  CK(h, cudaMalloc((void **)&ns_dev, sizeof(ns)));
+  cudaError_t e = se2p::launch_wait_expiry_test(h->err_dev, ns_dev, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(&ns, ns_dev, sizeof(ns), cudaMemcpyDeviceToHost);
+  cudaFree(ns_dev);
+  CK(h, e);
+  if (seconds) *seconds = 1e-9 * (double)ns;
+  return check_err_flag(h);
+}
+
 // ---------------------------------------------------------------- FP64 (tiled, reference order)
 static se2::StepParams<double> f64_params(se2gpu_solver *h)
 {

@@ -250,4 +250,29 @@ cudaError_t launch_norms(const float2 *u, const float2 *w, const float2 *cu, con
   return cudaGetLastError();
 }
 
+// The step kernels' bounded wait and error flag, on an mbarrier that nothing arrives
+// at: the wait gives up after EXPIRY_TEST_POLLS polls and the kernel raises the flag,
+// as a step kernel does when its tile copies never land.  No copy is in flight, so
+// the CTA exits normally.  ns[0] = the wait's duration (globaltimer).
+__global__ void wait_expiry_test(int *err, unsigned long long *ns)
+{
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x != 0) return;
+  const uint32_t b = smem_u32(&bar);
+  mbar_init(b, 1);
+  fence_barrier_init();
+  unsigned long long t0, t1;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  const bool ok = mbar_wait_bounded<EXPIRY_TEST_POLLS>(b, 0);
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+  if (!ok) atomicExch(err, 1);
+  ns[0] = t1 - t0;
+}
+
+cudaError_t launch_wait_expiry_test(int *err, unsigned long long *ns, cudaStream_t st)
+{
+  wait_expiry_test<<<1, 32, 0, st>>>(err, ns);
+  return cudaGetLastError();
+}
+
 }  // namespace se2p

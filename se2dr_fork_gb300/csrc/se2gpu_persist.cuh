@@ -88,11 +88,15 @@ __device__ __forceinline__ void prefetch_map(const CUtensorMap *map)
   asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)map) : "memory");
 }
 
-// bounded wait on a tile's copies
-constexpr long WAIT_LIMIT = 1L << 24;
+// bounded wait on a tile's copies (LIMIT polls; a smaller limit serves the expiry
+// self-test).  A poll of a barrier whose phase does not complete returns after the
+// hardware's suspend limit, measured at 3.75 us on GB300, so 2^18 polls give up
+// after about one second; copies that land take microseconds.
+constexpr long WAIT_LIMIT = 1L << 18;
+template <long LIMIT = WAIT_LIMIT>
 __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity)
 {
-  for (long i = 0; i < WAIT_LIMIT; i++)
+  for (long i = 0; i < LIMIT; i++)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }

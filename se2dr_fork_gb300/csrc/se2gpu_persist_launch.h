@@ -29,5 +29,9 @@ cudaError_t launch_record_batch(int p, const Params *shots, int nshots, int kblk
 int make_map(CUtensorMap *map, void *base, int nx, int ny, int pitch, int bw, int bh);
 cudaError_t launch_norms(const float2 *u, const float2 *w, const float2 *cu, const float2 *cw, const float2 *a, int nx,
                          int ny, int pitch, double dt, double *part, int nblocks, cudaStream_t st);
+// the bounded wait on a barrier nothing arrives at (EXPIRY_TEST_POLLS polls): raises
+// *err and writes the wait's duration in ns to *ns
+constexpr long EXPIRY_TEST_POLLS = 256;
+cudaError_t launch_wait_expiry_test(int *err, unsigned long long *ns, cudaStream_t st);
 
 }  // namespace se2p

@@ -22,7 +22,7 @@ PRECISIONS = {"fp64": FP64, "fp32_kahan": FP32_KAHAN, "fp32": FP32}
 
 # symbols declared in include/se2gpu.h
 EXPORTS = ["se2gpu_create", "se2gpu_destroy", "se2gpu_last_error", "se2gpu_create_error", "se2gpu_set_stream",
-           "se2gpu_synchronize", "se2gpu_set_fields", "se2gpu_get_fields", "se2gpu_advance", "se2gpu_traces",
+           "se2gpu_synchronize", "se2gpu_selftest_wait_expiry", "se2gpu_set_fields", "se2gpu_get_fields", "se2gpu_advance", "se2gpu_traces",
            "se2gpu_norms", "se2gpu_assemble_linear_form", "se2gpu_assemble_linear_form_device", "se2gpu_info",
            "se2gpu_device_fields", "se2gpu_tile_configs", "se2gpu_tile_config_info", "se2gpu_set_tile_config",
            "se2gpu_ensemble_create", "se2gpu_ensemble_destroy", "se2gpu_ensemble_last_error",
@@ -63,6 +63,7 @@ def lib():
         L.se2gpu_create_error.restype = C.c_char_p
         L.se2gpu_set_stream.argtypes = [vp, vp]
         L.se2gpu_synchronize.argtypes = [vp]
+        L.se2gpu_selftest_wait_expiry.argtypes = [vp, _dp]
         L.se2gpu_set_fields.argtypes = [vp, _dp, _dp, _dp]
         L.se2gpu_get_fields.argtypes = [vp, _dp, _dp, _dp]
         L.se2gpu_advance.argtypes = [vp, C.c_int, _dp]
@@ -217,6 +218,13 @@ class Solver:
     def set_fields(self, u=None, v=None, a=None):
         arrs = [None if x is None else np.ascontiguousarray(x, dtype=np.float64) for x in (u, v, a)]
         self._check(lib().se2gpu_set_fields(self._h, *[_p(x) for x in arrs]), "se2gpu_set_fields")
+
+    def selftest_wait_expiry(self):
+        """Run the step kernels' bounded wait on a barrier nothing arrives at.  Returns
+        (status, seconds the wait took, message); the handle is failed afterwards."""
+        sec = C.c_double(0.0)
+        rc = lib().se2gpu_selftest_wait_expiry(self._h, C.byref(sec))
+        return rc, sec.value, lib().se2gpu_last_error(self._h).decode()
 
     def norms(self) -> np.ndarray:
         out = np.zeros(6)
