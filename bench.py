@@ -350,7 +350,6 @@ def run_sweep(args):
     for p, mx in zip(range(1, 9), [4000, 2000, 1333, 1000, 800, 667, 571, 500]):
         vp = H.gaussian_random_field(mx, mx, 5000.0, 0.1, 8.0, seed=2048)
         sp = S.grf2048(mx, mx, p=p, nt=10 ** 6, cells=(vp, vp / 1.73, np.full_like(vp, 2700.0)))
-        sp = sp.replace(nearest_internal_gll=(p > 1))
         setup = H.Setup(sp)
         for prec in ["fp32_kahan", "fp64"]:
             k = args.steps if prec != "fp64" else max(3, args.steps // 10)

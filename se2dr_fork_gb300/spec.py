@@ -151,7 +151,9 @@ def grf2048(mx: int = 2048, my: Optional[int] = None, p: int = 4, nt: int = 2000
             cells: Optional[Tuple[np.ndarray, np.ndarray, np.ndarray]] = None) -> Spec:
     """20 km square with a Gaussian-random-field Vp (mean 5000, 10 % std, correlation
     length 8 cells), Vp/Vs = 1.73, rho = 2700; explosive Ricker f0 = 8 Hz source at the
-    centre; 64 receivers on the line y = +2500 m, x in [-8000, 8000]."""
+    centre; 64 receivers on the line y = +2500 m, x in [-8000, 8000].  Degree 1 has no
+    element-interior GLL point, so there the source and receivers snap to the nearest
+    node (the reference's -use_nearest_internal_gll false)."""
     my = mx if my is None else my
     if cells is None:
         from . import host  # C generator in the host library
@@ -161,7 +163,7 @@ def grf2048(mx: int = 2048, my: Optional[int] = None, p: int = 4, nt: int = 2000
     return Spec(mx=mx, my=my, p=p, scale=(20000.0, 20000.0), shift=(-10000.0, -10000.0),
                 vp=5000.0, vs=5000.0 / 1.73, rho=2700.0,
                 cell_vp=cells[0], cell_vs=cells[1], cell_rho=cells[2],
-                cfl=0.2, tmax=1.0e30, nt=nt, name="grf2048",
+                cfl=0.2, tmax=1.0e30, nt=nt, name="grf2048", nearest_internal_gll=(p > 1),
                 sources=[Source(0.0, 0.0, (1e15, 0.0, 0.0, 1e15), STF_RICKER, (0.15, 8.0, 1.0))],
                 receivers=rec)
 
