@@ -77,7 +77,6 @@ static int dzero(se2gpu_solver *h, void **p, size_t bytes)
   return 0;
 }
 
-// upload an FP64 host array in the handle's compute precision
 // fn(begin, end) over [0, n) on up to 16 host threads (at least minchunk items each): the
 // per-node host passes over meshes of tens of millions of nodes
 template <class F>
@@ -195,6 +194,7 @@ static int copy_f64(se2gpu_solver *h, double *dst, const double *src, size_t n, 
   return 0;
 }
 
+// upload an FP64 host array in the handle's compute precision
 static int upload(se2gpu_solver *h, void **dst, const double *src, size_t n)
 {
   int rc = dalloc(h, dst, n * h->tsize);
