@@ -985,12 +985,14 @@ extern "C" int se2gpu_checkpoint_load(se2gpu_solver *h, const void *buf, long by
   if (hd.precision != h->precision || hd.mx != h->mx || hd.my != h->my || hd.p != h->p || hd.nrec != h->nrec ||
       hd.pitch != h->pitch || hd.nnodes != h->nnodes)
     return fail(h, SE2GPU_ERR_ARG, "checkpoint of another problem or precision (%dx%d p%d precision %d)", hd.mx, hd.my, hd.p, hd.precision);
+  // the size does not depend on the state switched below: reject a truncated buffer
+  // before the handle is touched
+  if (bytes < se2gpu_checkpoint_size(h)) return fail(h, SE2GPU_ERR_ARG, "checkpoint truncated");
   CK(h, cudaSetDevice(h->device));
   CK(h, cudaStreamSynchronize(h->stream));
   h->rows_written = 0;
   h->pending_record = hd.pending_record != 0;
   if (!is_f64(h)) h->rlast = hd.rlast & 1;
-  if (bytes < se2gpu_checkpoint_size(h)) return fail(h, SE2GPU_ERR_ARG, "checkpoint truncated");
   const char *o = static_cast<const char *>(buf) + sizeof(hd);
   for (auto &a : state_arrays(h)) {
     CK(h, cudaMemcpy(a.first, o, a.second, cudaMemcpyHostToDevice));

@@ -355,6 +355,13 @@ def test_checkpoint_rejects_other_problems_and_buffered_rows():
         other.restore(blob)
     with pytest.raises(G.GpuError, match="another problem"):
         G.Solver(s1, "fp32").restore(blob)
+    # a truncated buffer is rejected before the handle is touched: the full one loads after it
+    n = G.lib().se2gpu_checkpoint_size(a.handle)
+    b = G.Solver(s1, "fp64")
+    assert G.lib().se2gpu_checkpoint_load(b.handle, blob[:n], n - 8) < 0
+    assert "truncated" in G.lib().se2gpu_last_error(b.handle).decode()
+    b.restore(blob)
+    assert np.array_equal(b.run(5)[:, 1:], a.run(5)[:, 1:])
 
 
 @pytest.mark.parametrize("impl", [0, 2, 3])
