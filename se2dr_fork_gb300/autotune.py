@@ -15,7 +15,7 @@ import math
 import os
 from typing import Dict, Optional
 
-from .gpu import Solver
+from .gpu import PRECISIONS, Solver
 
 CACHE = os.environ.get("SE2GPU_TUNING", os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning.json"))
 
@@ -88,8 +88,11 @@ def lookup(setup, precision: str) -> Optional[int]:
     return None if ent is None else int(ent["config"])
 
 
-def apply(sol: Solver, precision: str) -> int:
-    """Select the cached best configuration for this solver (configuration 0 if none)."""
+def apply(sol: Solver, precision: Optional[str] = None) -> int:
+    """Select the cached best configuration for this solver (configuration 0 if none).
+    `precision` defaults to the solver's own."""
+    if precision is None:
+        precision = {v: k for k, v in PRECISIONS.items()}[sol.precision]
     c = lookup(sol.setup, precision)
     if c is not None and c < len(sol.tile_configs()):
         sol.set_tile_config(c)
