@@ -153,6 +153,22 @@ def test_fp64_norms_vs_oracle():
     np.testing.assert_allclose(sol.norms(), last, rtol=1e-12, atol=0)
 
 
+@pytest.mark.parametrize("bad", [np.nan, np.inf])
+@pytest.mark.parametrize("precision", ["fp64", "fp32_kahan"])
+def test_norms_report_non_finite_fields(precision, bad):
+    """The log norms (se2wave.c:4747-4755) double as the blow-up detector: a non-finite
+    value injected into the host fields before upload comes back as SE2GPU_ERR_NUMERIC."""
+    setup = H.Setup(S.demo(6, 6, p=3, tmax=1.0).replace(nt=10))
+    sol = G.Solver(setup, precision)
+    sol.run(3)
+    u, v, a = sol.fields()
+    assert np.all(np.isfinite(sol.norms()))
+    u[setup.ndof // 3] = bad
+    sol.set_fields(u, v, a)
+    with pytest.raises(G.GpuError, match="non-finite"):
+        sol.norms()
+
+
 def test_fp64_set_fields_then_step_matches_oracle():
     sp = S.demo(6, 6, p=5, tmax=1.0).replace(nt=10)
     setup = H.Setup(sp)
