@@ -163,3 +163,28 @@ def test_app_interp_receiver_file_matches_reference(app, tmp_path, p):
     sta = np.loadtxt(tmp_path / f"closestqpsource-receiverCP-uva-{mx}x{my}-p{p}-rank0.dat", comments="#")
     assert sta.shape == (g["traces"].shape[0], 1 + 7 * 3)
     np.testing.assert_allclose(sta[:, 1:], g["traces"][:, 1:], rtol=1e-8, atol=1e-30)
+
+
+@pytest.mark.parametrize("args,message", [
+    (["-verify_stf"], "No STF implementation specified. Use one of { -stf_ricker , -stf_yoffe }"),   # se2wave.c:4825
+    (["-bdegree", "1"], "Cannot use basis degree = 1 and approximate the source location based on nearest "
+                        "cell interior GLL point"),                                                      # se2wave.c:3129
+    (["-precision", "fp16"], "unknown -precision fp16"),
+    (["-of", "0"], "-of must be at least 1"),
+    (["-source_impl", "7"], "-source_impl: valid choices are 0,1,2,3"),
+    (["-interp_receiver", "100"], "-interp_receiver: expected x,y"),
+])
+def test_app_rejects_bad_options_before_the_gpu(tmp_path, args, message):
+    """Option and set-up errors are reported (exit status 1, message on stderr) by the host
+    code, before any device work; the reference's own messages where it has them."""
+    from se2dr_fork_gb300 import build as B
+    B.build_host()
+    try:
+        B.build_gpu()
+        B.build_app()
+    except Exception as e:  # pragma: no cover - nvcc is part of the build environment
+        pytest.skip(f"application not buildable here: {e}")
+    r = subprocess.run([APP, "-mx", "4", *args], cwd=tmp_path, capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1
+    assert message in r.stderr, r.stderr
+    assert not any(f.endswith(".dat") for f in os.listdir(tmp_path))
