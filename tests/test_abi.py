@@ -117,3 +117,27 @@ def test_create_validates_the_problem_without_gpu(gpu_lib, case):
         rc = gpu.lib().se2gpu_create(ctypes.byref(pr), precision, cap, ctypes.byref(h))
         assert rc == -1 and not h.value, case
         assert msg in gpu.lib().se2gpu_create_error(), gpu.lib().se2gpu_create_error()
+
+
+@pytest.mark.parametrize("case", ["no_shots", "fp64", "block_zero", "block_too_long", "null_out"])
+def test_ensemble_create_validates_arguments_without_gpu(gpu_lib, case):
+    """The batched ensemble's argument checks run on the host before any device call."""
+    from se2dr_fork_gb300 import gpu
+    su, pr, keep = _small_problem()
+    shots = (gpu._CProblem * 1)(pr)
+    nshots, precision, block, msg = 1, 33, 100, None
+    if case == "no_shots":
+        nshots, msg = 0, b"at least one shot"
+    elif case == "fp64":
+        precision, msg = 64, b"FP32 precisions only"
+    elif case == "block_zero":
+        block, msg = 0, b"outside 1..4096"
+    elif case == "block_too_long":
+        block, msg = 4097, b"outside 1..4096"
+    else:
+        msg = b"null output handle"
+    h = ctypes.c_void_p()
+    out = None if case == "null_out" else ctypes.byref(h)
+    rc = gpu.lib().se2gpu_ensemble_create(shots, nshots, precision, block, out)
+    assert rc == -1 and not h.value, case
+    assert msg in gpu.lib().se2gpu_ensemble_last_error(None)
