@@ -141,3 +141,21 @@ def test_ensemble_create_validates_arguments_without_gpu(gpu_lib, case):
     rc = gpu.lib().se2gpu_ensemble_create(shots, nshots, precision, block, out)
     assert rc == -1 and not h.value, case
     assert msg in gpu.lib().se2gpu_ensemble_last_error(None)
+
+
+@pytest.mark.parametrize("change,msg", [
+    (dict(width=24), b"invalid network configuration"),       # not a multiple of 16 (tensor-core tiles)
+    (dict(cin=8), b"invalid network configuration"),
+    (dict(modes=65), b"invalid network configuration"),       # more modes than the grid resolves
+    (dict(nout=100), b"invalid network configuration"),       # not a multiple of the grid rows
+    (dict(max_batch=0), b"invalid network configuration"),
+    (dict(max_batch=256), b"batch too large for the launch grid"),
+])
+def test_surrogate_create_validates_the_configuration_without_gpu(nn_lib, change, msg):
+    """se2nn_create checks the network shape on the host before any device call."""
+    import dataclasses
+    from se2dr_fork_gb300 import nn
+    cfg = dataclasses.replace(nn.Config(), **change).c()
+    h = ctypes.c_void_p()
+    assert nn.lib().se2nn_create(ctypes.byref(cfg), 0, ctypes.byref(h)) == -1 and not h.value
+    assert msg in nn.lib().se2nn_last_error(None)
