@@ -159,3 +159,17 @@ def test_surrogate_create_validates_the_configuration_without_gpu(nn_lib, change
     h = ctypes.c_void_p()
     assert nn.lib().se2nn_create(ctypes.byref(cfg), 0, ctypes.byref(h)) == -1 and not h.value
     assert msg in nn.lib().se2nn_last_error(None)
+
+
+@pytest.mark.parametrize("n,msg", [(0, b"at least 1"), (-5, b"at least 1"),
+                                   ((1 << 28) + 1, b"exceeds the scratch limit")])
+def test_noalloc_norms_reject_bad_lengths_without_gpu(gpu_lib, n, msg):
+    """The allocation-free norms refuse lengths outside 1..2^28 before touching the device
+    (the pointers are never dereferenced on these paths)."""
+    from se2dr_fork_gb300 import gpu
+    out = (ctypes.c_double * 6)()
+    rc = gpu.lib().se2gpu_norms_device_noalloc(ctypes.c_void_p(256), ctypes.c_void_p(512), n, None, out)
+    assert rc == -1
+    assert msg in gpu.lib().se2gpu_last_error(None)
+    assert gpu.lib().se2gpu_norms_device_noalloc(None, ctypes.c_void_p(512), 10, None, out) == -1
+    assert b"null argument" in gpu.lib().se2gpu_last_error(None)
