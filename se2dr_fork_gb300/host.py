@@ -80,6 +80,8 @@ def lib():
         L.se2_interp_rows.argtypes = [C.POINTER(_CSetup), C.c_long, _dp, _dp]
         L.se2_shot_draw_params.argtypes = [C.c_ulonglong, C.c_long, C.c_int, C.POINTER(CShotDraw)]
         L.se2_shot_materials.argtypes = [C.POINTER(CShotDraw), _dp, _dp, _dp]
+        L.se2_write_vts.argtypes = [C.POINTER(_CSetup), C.c_char_p, C.c_int, C.POINTER(C.c_char_p),
+                                    C.POINTER(_dp)]
         _lib = L
     return _lib
 
@@ -224,6 +226,18 @@ class Setup:
         if lib().se2_interp_rows(self._ptr, rows.shape[0], _p(rows), _p(out)) != 0:
             raise ValueError(_err())
         return out
+
+    def write_vts(self, path: str, fields: dict):
+        """se2_write_vts: a VTK StructuredGrid snapshot over the GLL nodes of nodal fields
+        {name: interleaved [node][component] array of 2*nnodes}, arrays <name>_x, <name>_y."""
+        names = list(fields)
+        arrs = [np.ascontiguousarray(fields[k], dtype=np.float64) for k in names]
+        if any(a.size != self.ndof for a in arrs):
+            raise ValueError(f"every field needs {self.ndof} values")
+        cn = (C.c_char_p * len(names))(*[k.encode() for k in names])
+        cv = (_dp * len(arrs))(*[_p(a) for a in arrs])
+        if lib().se2_write_vts(self._ptr, str(path).encode(), len(names), cn, cv) != 0:
+            raise ValueError(_err())
 
     def stf_block(self, time: float, n: int) -> Tuple[np.ndarray, np.ndarray, float]:
         """Times and STF values of the next n steps after `time`."""

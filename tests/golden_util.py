@@ -65,3 +65,19 @@ def fp32_errors_ok(tr32, tr64, k=K_SHEAR):
 def rel_l2(x, ref):
     den = np.linalg.norm(ref)
     return np.linalg.norm(x - ref) / (den if den > 0 else 1.0)
+
+
+def read_vts(path):
+    """Arrays of a VTK XML StructuredGrid file with raw appended data (UInt64 headers)."""
+    import re
+    blob = open(path, "rb").read()
+    head, _, tail = blob.partition(b"<AppendedData encoding=\"raw\">")
+    data = tail[tail.index(b"_") + 1:]
+    ext = [int(v) for v in re.search(rb'WholeExtent="([^"]+)"', head).group(1).split()]
+    out = {}
+    for m in re.finditer(rb'<DataArray type="Float64" Name="([^"]+)" NumberOfComponents="(\d)" format="appended" '
+                         rb'offset="(\d+)"', head):
+        name, nc, off = m.group(1).decode(), int(m.group(2)), int(m.group(3))
+        nbytes = int(np.frombuffer(data[off:off + 8], dtype=np.uint64)[0])
+        out[name] = np.frombuffer(data[off + 8:off + 8 + nbytes], dtype=np.float64).reshape(-1, nc)
+    return (ext[1] + 1, ext[3] + 1), out

@@ -7,7 +7,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from golden_util import load
+from golden_util import load, read_vts
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 APP = os.path.join(ROOT, "se2dr_fork_gb300", "bin", "se2wave_gpu")
@@ -63,22 +63,6 @@ def test_app_verify_stf_matches_reference_ricker(tmp_path):
     from oracle import oracle as O
     ref = O.stf(0, (0.15, 12.0, 1.0), 0.0, 1.0e-4, 101)  # the literals the reference uses (se2wave.c:4837)
     np.testing.assert_allclose(vals, ref, rtol=1e-11, atol=1e-300)
-
-
-def read_vts(path):
-    """Arrays of a VTK XML StructuredGrid file with raw appended data (UInt64 headers)."""
-    import re
-    blob = open(path, "rb").read()
-    head, _, tail = blob.partition(b"<AppendedData encoding=\"raw\">")
-    data = tail[tail.index(b"_") + 1:]
-    ext = [int(v) for v in re.search(rb'WholeExtent="([^"]+)"', head).group(1).split()]
-    out = {}
-    for m in re.finditer(rb'<DataArray type="Float64" Name="([^"]+)" NumberOfComponents="(\d)" format="appended" '
-                         rb'offset="(\d+)"', head):
-        name, nc, off = m.group(1).decode(), int(m.group(2)), int(m.group(3))
-        nbytes = int(np.frombuffer(data[off:off + 8], dtype=np.uint64)[0])
-        out[name] = np.frombuffer(data[off + 8:off + 8 + nbytes], dtype=np.float64).reshape(-1, nc)
-    return (ext[1] + 1, ext[3] + 1), out
 
 
 @pytest.mark.gpu

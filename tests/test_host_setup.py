@@ -218,3 +218,23 @@ def test_interp_receiver_rejects_points_outside_the_mesh():
             H.Setup(sp.replace(interp_receivers=[xy]))
     e, N, xri = su.interp_receiver((-1000.0, -1000.0))     # the domain corner: element 0, xi = eta = -1
     assert e == 0 and N[0] == 1.0 and np.all(N[1:] == 0.0)
+
+
+def test_write_vts_round_trip(tmp_path):
+    """se2_write_vts (the VecView to a VTK viewer of se2wave.c:4764-4770): the grid extent,
+    the node positions and every component come back bit for bit."""
+    from golden_util import read_vts
+    su = H.Setup(S.demo(5, 3, p=3))
+    rng = np.random.default_rng(11)
+    u, v = rng.standard_normal(su.ndof), rng.standard_normal(su.ndof)
+    su.write_vts(tmp_path / "snap.vts", {"disp": u, "velo": v})
+    (nx, ny), arrs = read_vts(tmp_path / "snap.vts")
+    assert (nx, ny) == (su.nx_g, su.ny_g)
+    assert set(arrs) == {"Position", "disp_x", "disp_y", "velo_x", "velo_y"}
+    pos = arrs["Position"]
+    assert np.array_equal(pos[:, 0], np.tile(su.xnode, ny)) and np.array_equal(pos[:, 1], np.repeat(su.ynode, nx))
+    assert np.all(pos[:, 2] == 0)
+    for name, f in (("disp", u), ("velo", v)):
+        assert np.array_equal(arrs[name + "_x"][:, 0], f[0::2]) and np.array_equal(arrs[name + "_y"][:, 0], f[1::2])
+    with pytest.raises(ValueError):
+        su.write_vts(tmp_path / "bad.vts", {"disp": u[:-2]})
