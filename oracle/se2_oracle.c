@@ -1,8 +1,8 @@
 /*
  * se2_oracle.c -- CPU restatement of se2wave.c (Nicolucas/se2dr_fork).
  *
- * TEST INFRASTRUCTURE ONLY (parity checker and timed CPU baseline).  Every
- * function cites the reference lines it restates.  Floating-point expressions
+ * TEST INFRASTRUCTURE ONLY (the parity reference of the tests and the timed CPU
+ * baseline).  Every function cites the reference lines it restates.  Floating-point expressions
  * keep the reference's association and operand order; the file is compiled with
  * -ffp-contract=off so no multiply-add is fused.  PETSc semantics on one rank:
  * VecAXPY y = y + a*x (returns early for a == 0), VecPointwiseDivide w = x/y,

@@ -2,7 +2,7 @@
  * se2_oracle: CPU restatement of se2wave's explicit SEM time loop
  * (Nicolucas/se2dr_fork, se2wave.c).
  *
- * TEST INFRASTRUCTURE ONLY.  This is the parity checker for the GPU library and
+ * TEST INFRASTRUCTURE ONLY.  This is the parity reference for the GPU library and
  * the timed CPU baseline; the product never links or calls it.  It follows the
  * reference operation for operation (dense O(npe^2) element loop, per-element
  * derivative re-tabulation, ascending-element scatter-add, PETSc Vec semantics)
