@@ -3,7 +3,7 @@ reference itself) and with the oracle port, through the C-ABI.
 
 FP64 mode must be bit-identical (np.array_equal) to the reference; FP32 with
 Kahan-compensated updates must stay within 1e-5 relative L2 of the FP64
-receiver traces (the tolerance the target states for FP32).
+receiver traces (the FP32 trace tolerance).
 """
 import numpy as np
 import pytest
