@@ -172,3 +172,28 @@ def test_app_rejects_bad_options_before_the_gpu(tmp_path, args, message):
     assert r.returncode == 1
     assert message in r.stderr, r.stderr
     assert not any(f.endswith(".dat") for f in os.listdir(tmp_path))
+
+
+def test_app_rejects_bad_input_files_before_the_gpu(tmp_path):
+    """-rec_file and -cells are read on the host: a missing file, a short cell file and a
+    receiver outside the domain (the reference's message, se2wave.c:2727-2730) end the run
+    with exit status 1 before any device work."""
+    from se2dr_fork_gb300 import build as B
+    B.build_host()
+    try:
+        B.build_gpu()
+        B.build_app()
+    except Exception as e:  # pragma: no cover - nvcc is part of the build environment
+        pytest.skip(f"application not buildable here: {e}")
+
+    def run(*args):
+        return subprocess.run([APP, "-mx", "4", *args], cwd=tmp_path, capture_output=True, text=True, timeout=60)
+
+    r = run("-rec_file", "missing.txt")
+    assert r.returncode == 1 and "cannot open missing.txt" in r.stderr
+    np.zeros(47).tofile(tmp_path / "short.bin")          # 3 x 4 x 4 = 48 doubles are needed
+    r = run("-cells", "short.bin")
+    assert r.returncode == 1 and "cannot read 48 doubles from short.bin" in r.stderr
+    (tmp_path / "rec.txt").write_text("0.0 0.0\n1500.0 20.0\n")   # the demo's square is [-1000, 1000]^2
+    r = run("-rec_file", "rec.txt")
+    assert r.returncode == 1 and "Receiver 1, x-coordinate (+1.5000e+03) > max(domain).x (+1.0000e+03)" in r.stderr
