@@ -45,7 +45,7 @@ def peaks():
 # DRAM bytes per node and step of the step kernels as ncu measured them (dram__bytes_read.sum +
 # dram__bytes_write.sum of one launch at 1024^2, degree 4, divided by its 16.79M nodes; the
 # kernel's traffic grows in proportion to the nodes, so it is scaled to the workload's node
-# count): profiles/persist_step_fp32kahan_grf1024.md, profiles/step_kernel_fp64_grf512.md
+# count), from the ncu captures of the persistent FP32+Kahan step kernel at 1024^2
 MEASURED_TRAFFIC_PER_NODE = {"fp32_kahan": 1120.2e6 / 16785409}
 
 

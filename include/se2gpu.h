@@ -199,8 +199,11 @@ int se2gpu_ensemble_info(const se2gpu_ensemble *e, long *ints);
    array of SE2GPU_NOALLOC_MAX_BLOCKS x 6 doubles (192 KiB), so n may not exceed
    SE2GPU_NOALLOC_MAX_VALUES (larger n is rejected with SE2GPU_ERR_ARG).  The
    first call on each device looks up that array's address and should come
-   before any stream capture.  Calls that overlap in time share the array and
-   race.  On failure se2gpu_last_error(NULL) gives the message. */
+   before any stream capture; the address is kept until the process exits, so
+   the device must not be reset (cudaDeviceReset) while the library is loaded.
+   Calls that overlap in time share the array and race.  A NaN or Inf in u or v
+   makes an l2 norm non-finite and fails the call with SE2GPU_ERR_NUMERIC, as
+   se2gpu_norms does.  On failure se2gpu_last_error(NULL) gives the message. */
 #define SE2GPU_NOALLOC_CHUNK 65536L
 #define SE2GPU_NOALLOC_MAX_BLOCKS 4096
 #define SE2GPU_NOALLOC_MAX_VALUES (SE2GPU_NOALLOC_CHUNK * SE2GPU_NOALLOC_MAX_BLOCKS)

@@ -187,11 +187,13 @@ def bench(spec, nthreads: int, warmup: int, nsteps: int, record: bool = True) ->
 # ---------------------------------------------------------------------------
 # the reference itself, compiled in place (only where the reference tree exists)
 # ---------------------------------------------------------------------------
-def build_ref(refdir: str = "/root/reference") -> bool:
-    if not os.path.exists(os.path.join(refdir, "se2wave.c")):
-        return False
-    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFDIR={refdir}"], check=True, stdout=subprocess.DEVNULL)
-    return True
+def build_ref(refdir: Optional[str] = None) -> bool:
+    """Compile the reference in place (oracle/Makefile target ref-if-present) from refdir,
+    else from the SE2_REFERENCE_DIR environment variable, else from the recipe's default
+    tree.  Returns whether the driver exists afterwards."""
+    extra = [f"REFDIR={refdir}"] if refdir else []
+    subprocess.run(["make", "-s", "-C", HERE, "ref-if-present", *extra], check=True, stdout=subprocess.DEVNULL)
+    return os.path.exists(REF_DRIVER)
 
 
 def ref_source_vector(spec, impl: int, extra_args=()) -> np.ndarray:

@@ -409,7 +409,7 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
   }
   {
     // the tiled kernels serve FP64 and the FP32 internal-force entry point
-    cudaError_t e = (precision == SE2GPU_FP64) ? se2::prepare_f64(P->p) : se2::prepare_f32(P->p, false);
+    cudaError_t e = (precision == SE2GPU_FP64) ? se2::prepare_f64(P->p) : se2::prepare_f32(P->p);
     if (e != cudaSuccess) { fail(h, SE2GPU_ERR_CUDA, "kernel set-up: %s", cudaGetErrorString(e)); TRY(SE2GPU_ERR_CUDA); }
   }
   TRY(upload(h, &h->lam, P->lambda, (size_t)ne));
@@ -805,7 +805,7 @@ static int force_t(se2gpu_solver *h, const void *u_dev, void *F_dev)
   h->launches++;
   cudaError_t e;
   if constexpr (sizeof(T) == 8) e = se2::launch_step_f64(h->p, prm, h->nblocks - 1, h->stream);
-  else e = se2::launch_step_f32(h->p, false, prm, h->nblocks - 1, h->stream);
+  else e = se2::launch_step_f32(h->p, prm, h->nblocks - 1, h->stream);
   if (e != cudaSuccess) return fail(h, SE2GPU_ERR_CUDA, "force kernel: %s", cudaGetErrorString(e));
   return 0;
 }

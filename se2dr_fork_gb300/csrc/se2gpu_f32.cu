@@ -1,34 +1,24 @@
-// se2gpu_f32.cu -- FP32 instantiations (plain and Kahan-compensated), degrees 1..8.
+// se2gpu_f32.cu -- FP32 instantiations of the tiled step kernel, degrees 1..8.  They
+// serve the FP32 internal-force entry point (se2gpu_assemble_linear_form[_device] on
+// an FP32 handle, plain arithmetic); FP32 time stepping runs the persistent kernels of
+// se2gpu_f32p.cu.
 #include "se2gpu_launch.h"
 
 namespace se2 {
 
-template <int P, bool K>
-static cudaError_t prep1()
-{
-  return cudaFuncSetAttribute(step_kernel<P, float, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)smem_layout<P, float, K>().total);
-}
 template <int P>
-static cudaError_t prep(bool kahan) { return kahan ? prep1<P, true>() : prep1<P, false>(); }
+static cudaError_t prep()
+{
+  return cudaFuncSetAttribute(step_kernel<P, float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)smem_layout<P, float, false>().total);
+}
 
 template <int P>
-static cudaError_t launch(bool kahan, const StepParams<float> &prm, int nblocks, cudaStream_t st)
+static cudaError_t launch(const StepParams<float> &prm, int nblocks, cudaStream_t st)
 {
-  if (kahan) step_kernel<P, float, true><<<nblocks, 256, smem_layout<P, float, true>().total, st>>>(prm);
-  else step_kernel<P, float, false><<<nblocks, 256, smem_layout<P, float, false>().total, st>>>(prm);
+  step_kernel<P, float, false><<<nblocks, 256, smem_layout<P, float, false>().total, st>>>(prm);
   return cudaGetLastError();
 }
-
-template <int P>
-static cudaError_t record(const StepParams<float> &prm, cudaStream_t st)
-{
-  record_kernel<P, float><<<1, 128, 0, st>>>(prm);
-  return cudaGetLastError();
-}
-
-template <int P>
-static size_t smem(bool kahan) { return kahan ? smem_layout<P, float, true>().total : smem_layout<P, float, false>().total; }
 
 #define SE2_DISPATCH(fn, ...)                                               \
   switch (p) {                                                              \
@@ -39,13 +29,11 @@ static size_t smem(bool kahan) { return kahan ? smem_layout<P, float, true>().to
     default: break;                                                         \
   }
 
-cudaError_t prepare_f32(int p, bool kahan) { SE2_DISPATCH(prep, kahan) return cudaErrorInvalidValue; }
-cudaError_t launch_step_f32(int p, bool kahan, const StepParams<float> &prm, int nblocks, cudaStream_t st)
+cudaError_t prepare_f32(int p) { SE2_DISPATCH(prep) return cudaErrorInvalidValue; }
+cudaError_t launch_step_f32(int p, const StepParams<float> &prm, int nblocks, cudaStream_t st)
 {
-  SE2_DISPATCH(launch, kahan, prm, nblocks, st)
+  SE2_DISPATCH(launch, prm, nblocks, st)
   return cudaErrorInvalidValue;
 }
-cudaError_t launch_record_f32(int p, const StepParams<float> &prm, cudaStream_t st) { SE2_DISPATCH(record, prm, st) return cudaErrorInvalidValue; }
-size_t smem_f32(int p, bool kahan) { SE2_DISPATCH(smem, kahan) return 0; }
 
 }  // namespace se2

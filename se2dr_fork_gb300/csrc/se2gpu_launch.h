@@ -14,10 +14,8 @@ size_t smem_f64(int p);
 cudaError_t launch_step_f64(int p, const StepParams<double> &prm, int nblocks, cudaStream_t st);
 cudaError_t launch_record_f64(int p, const StepParams<double> &prm, cudaStream_t st);
 
-// FP32, plain or Kahan-compensated updates
-cudaError_t prepare_f32(int p, bool kahan);
-size_t smem_f32(int p, bool kahan);
-cudaError_t launch_step_f32(int p, bool kahan, const StepParams<float> &prm, int nblocks, cudaStream_t st);
-cudaError_t launch_record_f32(int p, const StepParams<float> &prm, cudaStream_t st);
+// FP32 internal force (plain arithmetic; FP32 stepping uses the persistent kernels)
+cudaError_t prepare_f32(int p);
+cudaError_t launch_step_f32(int p, const StepParams<float> &prm, int nblocks, cudaStream_t st);
 
 }  // namespace se2

@@ -11,7 +11,11 @@
 // block to finish (a ticket counter, cleared with cudaMemsetAsync before each
 // launch) reduces the partials in block order.  The result is therefore
 // independent of scheduling.  All calls share the one scratch array per device,
-// so calls that overlap in time (other streams or threads) race.
+// so calls that overlap in time (other streams or threads) race.  The looked-up
+// address is kept for the life of the process: it assumes the device is not
+// reset (cudaDeviceReset) while the library is loaded.  As se2gpu_norms does, a
+// non-finite l2 norm (a NaN or Inf anywhere in u or v) fails the call with
+// SE2GPU_ERR_NUMERIC: fmax/fmin skip NaN, so max and min alone could look finite.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -142,6 +146,9 @@ extern "C" int se2gpu_norms_device_noalloc(const double *u_dev, const double *v_
   if (rc) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int nb = (int)((n + kChunk - 1) / kChunk);
+  // a non-sticky error left by an earlier, unrelated call of the caller's is not this
+  // call's: clear it so that the launch check below reports this launch alone
+  (void)cudaGetLastError();
   cudaError_t e = cudaMemsetAsync(&sc->ticket, 0, sizeof(unsigned int), st);   // the ticket must start at zero
   if (e == cudaSuccess) {
     norms_noalloc<<<nb, kThreads, 0, st>>>(u_dev, v_dev, n, sc);
@@ -153,6 +160,11 @@ extern "C" int se2gpu_norms_device_noalloc(const double *u_dev, const double *v_
     char msg[256];
     snprintf(msg, sizeof(msg), "norms (no allocation): %s", cudaGetErrorString(e));
     return fail(SE2GPU_ERR_CUDA, msg);
+  }
+  if (!std::isfinite(out[2]) || !std::isfinite(out[5])) {
+    char msg[256];
+    snprintf(msg, sizeof(msg), "non-finite field norm (u l2 = %g, v l2 = %g)", out[2], out[5]);
+    return fail(SE2GPU_ERR_NUMERIC, msg);
   }
   return 0;
 }

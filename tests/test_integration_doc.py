@@ -1,4 +1,4 @@
-"""The C examples of INTEGRATION.md compile against include/*.h (gcc -fsyntax-only), with
+"""The C examples of the integration guide compile against include/*.h (gcc -fsyntax-only), with
 PETSc's names stubbed, so the documented calls keep matching the headers."""
 import os
 import re
