@@ -370,6 +370,59 @@ def run_sweep(args):
         del setup
 
 
+def trace_errors(tr, ref, k):
+    """Relative L2 of each receiver trace component (ux uy vx vy ax ay) against `ref`, and of
+    curl(v) on the scale k |v| of the velocity gradient (an explosive source's curl is
+    discretisation noise, so its own norm measures nothing)."""
+    errs = []
+    for c in range(6):
+        den = np.linalg.norm(ref[:, 1 + c::7])
+        errs.append(float(np.linalg.norm(tr[:, 1 + c::7] - ref[:, 1 + c::7]) / (den if den > 0 else 1.0)))
+    vn = np.sqrt(np.linalg.norm(ref[:, 3::7]) ** 2 + np.linalg.norm(ref[:, 4::7]) ** 2)
+    scale = max(np.linalg.norm(ref[:, 7::7]), k * vn)
+    errs.append(float(np.linalg.norm(tr[:, 7::7] - ref[:, 7::7]) / (scale if scale > 0 else 1.0)))
+    return errs
+
+
+def run_accuracy(args):
+    """FP32 modes against FP64 on the same problem over --steps steps: relative L2 of every
+    receiver trace component and of the final u, v, a fields, one JSON line per precision.
+    The 2048^2 degree-4 workload (64 receivers on y = 2500 m; its default 20000 steps reach
+    t = 1.04 s, past the P and S arrivals), or with --sweep the degree-sweep meshes."""
+    import torch
+    from se2dr_fork_gb300 import gpu as G
+    from se2dr_fork_gb300 import host as H
+    from se2dr_fork_gb300 import spec as S
+    torch.cuda.set_device(0)
+    cases = list(zip(range(1, 9), [4000, 2000, 1333, 1000, 800, 667, 571, 500])) if args.sweep else [(args.degree, args.mx)]
+    k_shear = 2.0 * np.pi * 8.0 / (5000.0 / 1.73)   # Ricker f0 over the mean shear speed
+    for p, mx in cases:
+        vp = H.gaussian_random_field(mx, mx, 5000.0, 0.1, 8.0, seed=2048)
+        setup = H.Setup(S.grf2048(mx, mx, p=p, nt=args.steps, cells=(vp, vp / 1.73, np.full_like(vp, 2700.0))))
+        ref = None
+        for prec in ["fp64", "fp32_df", "fp32_kahan", "fp32"]:
+            sol = G.Solver(setup, prec, trace_capacity=min(args.steps, 2000))
+            t0 = time.time()
+            tr = sol.run(args.steps, block=2000)
+            sol.synchronize()
+            secs = time.time() - t0
+            fields = sol.fields()
+            sol.close()
+            if prec == "fp64":
+                ref = (tr, fields)
+                errs, ferr = None, None
+            else:
+                errs = trace_errors(tr, ref[0], k_shear)
+                ferr = {n: float(np.linalg.norm(x - y) / np.linalg.norm(y)) for n, x, y in zip("uva", fields, ref[1])}
+            print(json.dumps({"accuracy": "sweep" if args.sweep else "grf2048", "p": p, "mx": mx, "nodes": setup.nnodes,
+                              "steps": args.steps, "t_end": float(tr[-1, 0]) if len(tr) else 0.0,
+                              "receivers": setup.nrec, "precision": prec, "wall_s": secs,
+                              "trace_rel_l2": dict(zip(["ux", "uy", "vx", "vy", "ax", "ay", "curl"], errs)) if errs else None,
+                              "field_rel_l2": ferr}), flush=True)
+            del fields
+        del setup, ref
+
+
 def run_ensemble(args, rank: int = 0, world: int = 1):
     """Batched ensemble: `--shots` seeded shots (mx, my ~ U{32..512}, p in {3,4,6}, 2 layers +
     elliptical inclusion, random source and moment tensor, Ricker f0 ~ U[5,20] Hz, 32 receivers,
@@ -639,12 +692,16 @@ def main():
     ap.add_argument("--threshold", type=float, default=0.01)
     ap.add_argument("--nn-step", action="store_true", help="time the surrogate's training step alone")
     ap.add_argument("--nn-batch", type=int, default=32)
+    ap.add_argument("--accuracy", action="store_true",
+                    help="FP32 modes against FP64 over --steps steps (error table) instead of the headline run")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     if args.warmup < 3:
         args.warmup = 3
-    if args.sweep:
+    if args.accuracy:
+        run_accuracy(args)
+    elif args.sweep:
         run_sweep(args)
     elif args.ensemble and args.impl == "ours":
         run_ensemble(args, rank, world)

@@ -34,6 +34,11 @@ extern "C" {
 #define SE2GPU_FP64        64  /* FP64, reference operation order, no fused multiply-add: bit-identical to the CPU reference */
 #define SE2GPU_FP32_KAHAN  33  /* FP32 arithmetic, Kahan-compensated u and v updates */
 #define SE2GPU_FP32        32  /* FP32 arithmetic, plain updates */
+#define SE2GPU_FP32_DF     34  /* two-float arithmetic: every value of a step (displacement differences, gradients,
+                                  stresses, forces, 1/M, the updates) carried as an unevaluated sum of two
+                                  floats, about 48 significant bits, on the FP32 pipe; state stored as in
+                                  SE2GPU_FP32_KAHAN, whose accelerations and curl(v) traces carry the FP32
+                                  force evaluation's rounding (1e-4 to 1e-3 relative L2 of FP64) */
 
 /* error codes */
 #define SE2GPU_OK            0
@@ -208,6 +213,15 @@ int se2gpu_ensemble_info(const se2gpu_ensemble *e, long *ints);
 #define SE2GPU_NOALLOC_MAX_BLOCKS 4096
 #define SE2GPU_NOALLOC_MAX_VALUES (SE2GPU_NOALLOC_CHUNK * SE2GPU_NOALLOC_MAX_BLOCKS)
 int se2gpu_norms_device_noalloc(const double *u_dev, const double *v_dev, long n, void *stream, double out[6]);
+
+/* ---- Arithmetic-pipe peak of the current device (no counterpart in the reference): the
+   roofline denominator of the kernels that HBM does not bound.  Measured with CUDA events
+   on independent dependency chains (4 CTAs of 256 threads per SM).  kind 0: FP64
+   separately rounded multiply + add (the operations of the FP64 step kernel, which
+   follows the reference's operation order and fuses nothing); 1: FP64 fused
+   multiply-add; 2: FP32 separately rounded multiply + add; 3: FP32 fused multiply-add.
+   *ops_per_second counts arithmetic operations (a fused multiply-add counts two). */
+int se2gpu_pipe_peak(int kind, double *ops_per_second);
 
 #ifdef __cplusplus
 }

@@ -31,7 +31,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-ffp-contract=off", f"-I{INC}"]
 CC_FLAGS = ["-O2", "-std=gnu99", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", f"-I{INC}"]
 
-CU_UNITS = ["se2gpu_f64", "se2gpu_f32", "se2gpu_f32p", "se2gpu_api", "se2gpu_ensemble", "se2gpu_noalloc"]
+CU_UNITS = ["se2gpu_f64", "se2gpu_f32", "se2gpu_f32p", "se2gpu_f32df", "se2gpu_api", "se2gpu_ensemble", "se2gpu_noalloc", "se2gpu_peaks"]
 CU_DEPS = ["se2gpu_kernels.cuh", "se2gpu_launch.h", "se2gpu_persist.cuh", "se2gpu_persist_launch.h", "se2gpu_persist_params.h", "se2gpu_internal.h"]
 
 

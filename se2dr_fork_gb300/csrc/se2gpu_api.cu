@@ -20,6 +20,7 @@
 #include <atomic>
 #include <climits>
 #include <memory>
+#include <mutex>
 #include <thread>
 #include <unistd.h>
 #include <utility>
@@ -55,25 +56,81 @@ static int fail(se2gpu_solver *h, int code, const char *fmt, ...)
   } while (0)
 
 static bool is_f64(const se2gpu_solver *h) { return h->precision == SE2GPU_FP64; }
-static bool is_kahan(const se2gpu_solver *h) { return h->precision == SE2GPU_FP32_KAHAN; }
+// FP32 modes that keep compensation terms of u and w (Kahan and two-float)
+static bool is_kahan(const se2gpu_solver *h) { return h->precision == SE2GPU_FP32_KAHAN || h->precision == SE2GPU_FP32_DF; }
+static bool is_df(const se2gpu_solver *h) { return h->precision == SE2GPU_FP32_DF; }
+// the persistent kernel's arithmetic mode
+static int pmode(const se2gpu_solver *h)
+{
+  return is_df(h) ? se2p::MODE_DF : (h->precision == SE2GPU_FP32_KAHAN) ? se2p::MODE_KAHAN : se2p::MODE_PLAIN;
+}
+// receiver side-buffer floats per element node: (u, v, a), with low parts in the two-float mode
+static int rbuf_values(const se2gpu_solver *h) { return is_df(h) ? 12 : 6; }
+// the two-float mode keeps the low parts of the last step's a after the high parts
+static float2 *pa_lo(const se2gpu_solver *h) { return is_df(h) ? h->pa + (size_t)h->ny_g * h->pitch : nullptr; }
+
+// Device memory of the handles comes from one stream-ordered pool per device whose
+// release threshold keeps freed memory for the next handle: a create that follows a
+// destroy in the same process maps no new memory, and allocations, frees and the
+// zeroing of the state are queued on the handle's stream without host waits.  When the
+// pool cannot grow, the memory it holds unused is returned to the device and the
+// allocation is tried once more.
+static cudaMemPool_t device_pool(int dev)
+{
+  static std::mutex mu;
+  static cudaMemPool_t pools[64];
+  static bool made[64];
+  if (dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!made[dev]) {
+    cudaMemPoolProps pr;
+    memset(&pr, 0, sizeof(pr));
+    pr.allocType = cudaMemAllocationTypePinned;
+    pr.location.type = cudaMemLocationTypeDevice;
+    pr.location.id = dev;
+    if (cudaMemPoolCreate(&pools[dev], &pr) != cudaSuccess) {
+      cudaGetLastError();
+      pools[dev] = nullptr;
+    } else {
+      cuuint64_t keep = ~(cuuint64_t)0;
+      cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    made[dev] = true;
+  }
+  return pools[dev];
+}
 
 static int dalloc(se2gpu_solver *h, void **p, size_t bytes)
 {
   *p = nullptr;
-  cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+  const size_t n = bytes ? bytes : 16;
+  cudaMemPool_t pool = device_pool(h->device);
+  cudaError_t e = pool ? cudaMallocFromPoolAsync(p, n, pool, h->stream) : cudaErrorMemoryAllocation;
+  if (e != cudaSuccess && pool) {
+    cudaGetLastError();
+    cudaStreamSynchronize(h->stream);
+    cudaMemPoolTrimTo(pool, 0);
+    e = cudaMallocFromPoolAsync(p, n, pool, h->stream);
+  }
   if (e != cudaSuccess) {
     *p = nullptr;
     cudaGetLastError();
-    return fail(h, SE2GPU_ERR_NOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+    return fail(h, SE2GPU_ERR_NOMEM, "device allocation of %zu bytes: %s", bytes, cudaGetErrorString(e));
   }
   return 0;
+}
+
+// free a handle allocation (null is ignored), ordered on the handle's stream
+static void dfree(se2gpu_solver *h, void *p)
+{
+  if (p) cudaFreeAsync(p, h->stream);
 }
 
 static int dzero(se2gpu_solver *h, void **p, size_t bytes)
 {
   int rc = dalloc(h, p, bytes);
   if (rc) return rc;
-  CK(h, cudaMemset(*p, 0, bytes ? bytes : 16));
+  CK(h, cudaMemsetAsync(*p, 0, bytes ? bytes : 16, h->stream));
   return 0;
 }
 
@@ -96,13 +153,20 @@ static void host_parallel(long n, F fn, long minchunk = 1L << 20)
 // 1/M in the padded FP32 layout (padding nodes 0) straight from the caller's FP64 mass,
 // for devices that read pageable host memory (cudaDevAttrPageableMemoryAccess).  Double
 // division and the conversion to float round as on the host, so the values are the same.
+// minv_lo (two-float mode, else null): the remainder 1/M - minv, rounded to float.  *bad
+// receives the smallest node whose mass is not positive and finite (it starts at ~0).
 __global__ void k_minv_from_host(const double *__restrict__ mass, long nx_g, long ny_g, int pitch,
-                                 float *__restrict__ minv)
+                                 float *__restrict__ minv, float *__restrict__ minv_lo, unsigned long long *bad)
 {
   const long np = ny_g * (long)pitch;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < np; i += (long)gridDim.x * blockDim.x) {
     const long y = i / pitch, x = i - y * pitch;
-    minv[i] = (x < nx_g) ? __double2float_rn(1.0 / mass[y * nx_g + x]) : 0.f;
+    const double m = (x < nx_g) ? mass[y * nx_g + x] : 1.0;
+    if (!(m > 0.0) || !isfinite(m)) atomicMin(bad, (unsigned long long)(y * nx_g + x));
+    const double r = (x < nx_g) ? 1.0 / m : 0.0;
+    const float h = __double2float_rn(r);
+    minv[i] = h;
+    if (minv_lo) minv_lo[i] = __double2float_rn(__dsub_rn(r, (double)h));
   }
 }
 
@@ -118,33 +182,36 @@ __global__ void k_copy_f64(double *__restrict__ dst, const double *__restrict__ 
 }
 
 // FP32 leapfrog state (padded rows) -> FP64 (u, v, a) in the reference's node order
+// (AL: the low parts of a in the two-float mode, else null)
 __global__ void k_fields_to_host(const float2 *__restrict__ U, const float2 *__restrict__ W,
                                  const float2 *__restrict__ CU, const float2 *__restrict__ CW,
-                                 const float2 *__restrict__ A, long nx_g, long ny_g, int pitch, double dt,
-                                 double hdt, double *u, double *v, double *a)
+                                 const float2 *__restrict__ A, const float2 *__restrict__ AL, long nx_g, long ny_g,
+                                 int pitch, double dt, double hdt, double *u, double *v, double *a)
 {
   const long nn = nx_g * ny_g;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nn; i += (long)gridDim.x * blockDim.x) {
     const long y = i / nx_g, x = i - y * nx_g, k = y * pitch + x;
-    const float2 w = W[k], uu = U[k], ac = A[k];
+    const float2 w = W[k], uu = U[k], ac = A[k], al = AL ? AL[k] : make_float2(0.f, 0.f);
     const float2 cw = CW ? CW[k] : make_float2(0.f, 0.f), cu = CU ? CU[k] : make_float2(0.f, 0.f);
     const double w0 = __dsub_rn((double)w.x, (double)cw.x), w1 = __dsub_rn((double)w.y, (double)cw.y);
     const double u0 = __dsub_rn((double)uu.x, (double)cu.x), u1 = __dsub_rn((double)uu.y, (double)cu.y);
+    const double a0 = __dadd_rn((double)ac.x, (double)al.x), a1 = __dadd_rn((double)ac.y, (double)al.y);
     if (u) { u[2 * i] = __dsub_rn(u0, __dmul_rn(dt, w0)); u[2 * i + 1] = __dsub_rn(u1, __dmul_rn(dt, w1)); }
-    if (v) { v[2 * i] = __dsub_rn(w0, __dmul_rn(hdt, (double)ac.x)); v[2 * i + 1] = __dsub_rn(w1, __dmul_rn(hdt, (double)ac.y)); }
-    if (a) { a[2 * i] = (double)ac.x; a[2 * i + 1] = (double)ac.y; }
+    if (v) { v[2 * i] = __dsub_rn(w0, __dmul_rn(hdt, a0)); v[2 * i + 1] = __dsub_rn(w1, __dmul_rn(hdt, a1)); }
+    if (a) { a[2 * i] = a0; a[2 * i + 1] = a1; }
   }
 }
 
 // FP64 (u, v, a) -> FP32 leapfrog state with its Kahan terms (padding nodes 0)
 __global__ void k_fields_from_host(const double *u, const double *v, const double *a, long nx_g, long ny_g,
                                    int pitch, double dt, double hdt, float2 *__restrict__ U, float2 *__restrict__ W,
-                                   float2 *__restrict__ CU, float2 *__restrict__ CW, float2 *__restrict__ A)
+                                   float2 *__restrict__ CU, float2 *__restrict__ CW, float2 *__restrict__ A,
+                                   float2 *__restrict__ AL)
 {
   const long np = ny_g * (long)pitch;
   for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < np; k += (long)gridDim.x * blockDim.x) {
     const long y = k / pitch, x = k - y * pitch;
-    float2 Wk = make_float2(0.f, 0.f), Uk = Wk, CWk = Wk, CUk = Wk, Ak = Wk;
+    float2 Wk = make_float2(0.f, 0.f), Uk = Wk, CWk = Wk, CUk = Wk, Ak = Wk, ALk = Wk;
     if (x < nx_g) {
       const long n = y * nx_g + x;
       double wv[2], uv[2];
@@ -158,8 +225,12 @@ __global__ void k_fields_from_host(const double *u, const double *v, const doubl
       CWk = make_float2(__double2float_rn(__dsub_rn((double)Wk.x, wv[0])), __double2float_rn(__dsub_rn((double)Wk.y, wv[1])));
       CUk = make_float2(__double2float_rn(__dsub_rn((double)Uk.x, uv[0])), __double2float_rn(__dsub_rn((double)Uk.y, uv[1])));
       Ak = make_float2(a ? __double2float_rn(a[2 * n]) : 0.f, a ? __double2float_rn(a[2 * n + 1]) : 0.f);
+      if (a && AL)
+        ALk = make_float2(__double2float_rn(__dsub_rn(a[2 * n], (double)Ak.x)),
+                          __double2float_rn(__dsub_rn(a[2 * n + 1], (double)Ak.y)));
     }
     U[k] = Uk; W[k] = Wk; A[k] = Ak;
+    if (AL) AL[k] = ALk;
     if (CU) { CU[k] = CUk; CW[k] = CWk; }
   }
 }
@@ -189,31 +260,58 @@ static int copy_f64(se2gpu_solver *h, double *dst, const double *src, size_t n, 
     CK(h, cudaGetLastError());
     CK(h, cudaStreamSynchronize(h->stream));
   } else {
-    CK(h, cudaMemcpy(dst, src, n * 8, kind));
+    CK(h, cudaMemcpyAsync(dst, src, n * 8, kind, h->stream));
   }
   return 0;
 }
 
-// upload an FP64 host array in the handle's compute precision
+// FP64 host array -> nearest floats (and, with lo, the remainders rounded to float), read
+// where it lies by a device that reads pageable host memory
+__global__ void k_to_float(const double *__restrict__ src, size_t n, float *__restrict__ dst, float *__restrict__ lo)
+{
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double v = src[i];
+    const float f = __double2float_rn(v);
+    dst[i] = f;
+    if (lo) lo[i] = __double2float_rn(__dsub_rn(v, (double)f));
+  }
+}
+
+// upload an FP64 host array in the handle's compute precision (two-float mode: the n
+// nearest floats followed by the n remainders, rounded to float).  FP32 tables on a
+// device that reads pageable host memory are converted by a kernel on the handle's
+// stream, which se2gpu_create synchronises once at its end (the caller's arrays stay
+// valid until it returns).
 static int upload(se2gpu_solver *h, void **dst, const double *src, size_t n)
 {
-  int rc = dalloc(h, dst, n * h->tsize);
+  const size_t nf = is_df(h) ? 2 * n : n;
+  int rc = dalloc(h, dst, nf * h->tsize);
   if (rc) return rc;
   if (h->tsize == 8) {
     return copy_f64(h, (double *)*dst, src, n, cudaMemcpyHostToDevice);
+  } else if (h->pageable && n) {
+    float *d = (float *)*dst;
+    k_to_float<<<(int)std::min<size_t>((n + 255) / 256, (size_t)4 * h->nsm), 256, 0, h->stream>>>(
+        src, n, d, nf > n ? d + n : nullptr);
+    CK(h, cudaGetLastError());
   } else {
-    std::vector<float> tmp(n);
-    for (size_t i = 0; i < n; i++) tmp[i] = (float)src[i];
-    CK(h, cudaMemcpy(*dst, tmp.data(), n * 4, cudaMemcpyHostToDevice));
+    std::vector<float> tmp(nf);
+    host_parallel((long)n, [&](long i0, long i1) {
+      for (long i = i0; i < i1; i++) tmp[i] = (float)src[i];
+      if (nf > n)
+        for (long i = i0; i < i1; i++) tmp[n + i] = (float)(src[i] - (double)tmp[i]);
+    });
+    if (nf) CK(h, cudaMemcpyAsync(*dst, tmp.data(), nf * 4, cudaMemcpyHostToDevice, h->stream));
   }
   return 0;
 }
 
+// (cudaMemcpyAsync from pageable host memory returns once the source has been staged)
 static int upload_d(se2gpu_solver *h, double **dst, const double *src, size_t n)
 {
   int rc = dalloc(h, (void **)dst, n * 8);
   if (rc) return rc;
-  CK(h, cudaMemcpy(*dst, src, n * 8, cudaMemcpyHostToDevice));
+  if (n) CK(h, cudaMemcpyAsync(*dst, src, n * 8, cudaMemcpyHostToDevice, h->stream));
   return 0;
 }
 
@@ -221,7 +319,7 @@ static int upload_i(se2gpu_solver *h, int **dst, const int *src, size_t n)
 {
   int rc = dalloc(h, (void **)dst, n * 4);
   if (rc) return rc;
-  if (n) CK(h, cudaMemcpy(*dst, src, n * 4, cudaMemcpyHostToDevice));
+  if (n) CK(h, cudaMemcpyAsync(*dst, src, n * 4, cudaMemcpyHostToDevice, h->stream));
   return 0;
 }
 
@@ -231,14 +329,15 @@ extern "C" void se2gpu_destroy(se2gpu_solver *h)
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (int b = 0; b < 2; b++) {
-    for (int f = 0; f < 3; f++) cudaFree(h->f64[b][f]);
-    cudaFree(h->pu[b]); cudaFree(h->pw[b]); cudaFree(h->pcu[b]); cudaFree(h->pcw[b]); cudaFree(h->rbuf[b]);
+    for (int f = 0; f < 3; f++) dfree(h, h->f64[b][f]);
+    dfree(h, h->pu[b]); dfree(h, h->pw[b]); dfree(h, h->pcu[b]); dfree(h, h->pcw[b]); dfree(h, h->rbuf[b]);
   }
-  void *ptrs[] = {h->pa, h->pminv, h->err_dev, h->mass, h->lam, h->mu, h->J00, h->J11, h->iJ00, h->iJ11, h->D, h->wq,
+  void *ptrs[] = {h->pa, h->pminv, h->mass_bad, h->err_dev, h->mass, h->lam, h->mu, h->J00, h->J11, h->iJ00, h->iJ11, h->D, h->wq,
                   h->src_vals, h->Dd, h->iJ00d, h->iJ11d, h->stf_dev, h->traces, h->norm_part, h->src_elem,
                   h->rec_node, h->rec_elem, h->rec_gll, h->scratch_u, h->scratch_f, h->tile_src_off,
                   h->tile_src_idx, h->tile_rec_off, h->tile_rec_idx};
-  for (void *p : ptrs) cudaFree(p);
+  for (void *p : ptrs) dfree(h, p);
+  if (h->stream) cudaStreamSynchronize(h->stream);   // the frees are done before the stream goes
   delete h->src_elem_h;
   delete h->rec_elem_h;
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -255,12 +354,12 @@ static int upload_leapfrog(se2gpu_solver *h, const double *u, const double *v, c
     const bool kahan = is_kahan(h);
     k_fields_from_host<<<4 * h->nsm, 256, 0, h->stream>>>(u, v, a, h->nx_g, h->ny_g, h->pitch, h->dt, 0.5 * h->dt,
                                                           h->pu[c], h->pw[c], kahan ? h->pcu[c] : nullptr,
-                                                          kahan ? h->pcw[c] : nullptr, h->pa);
+                                                          kahan ? h->pcw[c] : nullptr, h->pa, pa_lo(h));
     CK(h, cudaGetLastError());
     CK(h, cudaStreamSynchronize(h->stream));
     return 0;
   }
-  std::vector<float2> U(np), W(np), CU(np), CW(np), A(np);
+  std::vector<float2> U(np), W(np), CU(np), CW(np), A(np), AL(np, make_float2(0.f, 0.f));
   const double dt = h->dt, hdt = 0.5 * h->dt;
   for (long y = 0; y < h->ny_g; y++)
     for (long x = 0; x < h->nx_g; x++) {
@@ -276,15 +375,17 @@ static int upload_leapfrog(se2gpu_solver *h, const double *u, const double *v, c
       CW[k] = make_float2((float)((double)W[k].x - wv[0]), (float)((double)W[k].y - wv[1]));
       CU[k] = make_float2((float)((double)U[k].x - uv[0]), (float)((double)U[k].y - uv[1]));
       A[k] = make_float2(a ? (float)a[2 * n] : 0.f, a ? (float)a[2 * n + 1] : 0.f);
+      if (a) AL[k] = make_float2((float)(a[2 * n] - (double)A[k].x), (float)(a[2 * n + 1] - (double)A[k].y));
     }
   const int c = h->cur;
-  CK(h, cudaMemcpy(h->pu[c], U.data(), np * 8, cudaMemcpyHostToDevice));
-  CK(h, cudaMemcpy(h->pw[c], W.data(), np * 8, cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpyAsync(h->pu[c], U.data(), np * 8, cudaMemcpyHostToDevice, h->stream));
+  CK(h, cudaMemcpyAsync(h->pw[c], W.data(), np * 8, cudaMemcpyHostToDevice, h->stream));
   if (is_kahan(h)) {
-    CK(h, cudaMemcpy(h->pcu[c], CU.data(), np * 8, cudaMemcpyHostToDevice));
-    CK(h, cudaMemcpy(h->pcw[c], CW.data(), np * 8, cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpyAsync(h->pcu[c], CU.data(), np * 8, cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->pcw[c], CW.data(), np * 8, cudaMemcpyHostToDevice, h->stream));
   }
-  CK(h, cudaMemcpy(h->pa, A.data(), np * 8, cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpyAsync(h->pa, A.data(), np * 8, cudaMemcpyHostToDevice, h->stream));
+  if (pa_lo(h)) CK(h, cudaMemcpyAsync(pa_lo(h), AL.data(), np * 8, cudaMemcpyHostToDevice, h->stream));
   return 0;
 }
 
@@ -293,11 +394,12 @@ static int upload_leapfrog(se2gpu_solver *h, const double *u, const double *v, c
 static int setup_f32_config(se2gpu_solver *h, int config)
 {
   const bool kahan = is_kahan(h);
+  const int mode = pmode(h);
   se2p::TileShape ts;
-  if (se2p::config_shape(h->p, config, kahan, &ts)) return fail(h, SE2GPU_ERR_ARG, "no tile configuration %d for degree %d", config, h->p);
+  if (se2p::config_shape(h->p, config, mode, &ts)) return fail(h, SE2GPU_ERR_ARG, "no tile configuration %d for degree %d", config, h->p);
   CK(h, cudaStreamSynchronize(h->stream));
   {
-    cudaError_t e = se2p::prepare(h->p, config, kahan);
+    cudaError_t e = se2p::prepare(h->p, config, mode);
     if (e != cudaSuccess) return fail(h, SE2GPU_ERR_CUDA, "persistent kernel set-up: %s", cudaGetErrorString(e));
   }
   for (int b = 0; b < 2; b++) {
@@ -330,7 +432,7 @@ static int setup_f32_config(se2gpu_solver *h, int config)
   std::vector<int> so, si, ro, ri;
   build(*h->src_elem_h, so, si);
   build(*h->rec_elem_h, ro, ri);
-  cudaFree(h->tile_src_off); cudaFree(h->tile_src_idx); cudaFree(h->tile_rec_off); cudaFree(h->tile_rec_idx);
+  dfree(h, h->tile_src_off); dfree(h, h->tile_src_idx); dfree(h, h->tile_rec_off); dfree(h, h->tile_rec_idx);
   h->tile_src_off = h->tile_src_idx = h->tile_rec_off = h->tile_rec_idx = nullptr;
   int rc;
   if ((rc = upload_i(h, &h->tile_src_off, so.data(), so.size()))) return rc;
@@ -340,7 +442,7 @@ static int setup_f32_config(se2gpu_solver *h, int config)
   h->pconfig = config;
   h->pntx = ntx;
   h->pnty = nty;
-  h->pgrid = std::min(ntiles, std::max(1, se2p::occupancy(P, config, kahan)) * h->nsm);
+  h->pgrid = std::min(ntiles, std::max(1, se2p::occupancy(P, config, mode)) * h->nsm);
   return 0;
 }
 
@@ -349,8 +451,9 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
   if (!out) return fail(nullptr, SE2GPU_ERR_ARG, "null output handle");
   *out = nullptr;
   if (!P) return fail(nullptr, SE2GPU_ERR_ARG, "null problem");
-  if (precision != SE2GPU_FP64 && precision != SE2GPU_FP32 && precision != SE2GPU_FP32_KAHAN)
-    return fail(nullptr, SE2GPU_ERR_ARG, "unknown precision %d (use 64, 33 or 32)", precision);
+  if (precision != SE2GPU_FP64 && precision != SE2GPU_FP32 && precision != SE2GPU_FP32_KAHAN &&
+      precision != SE2GPU_FP32_DF)
+    return fail(nullptr, SE2GPU_ERR_ARG, "unknown precision %d (use 64, 34, 33 or 32)", precision);
   if (P->p < 1 || P->p > 8) return fail(nullptr, SE2GPU_ERR_ARG, "polynomial degree %d outside 1..8", P->p);
   if (P->mx < 1 || P->my < 1) return fail(nullptr, SE2GPU_ERR_ARG, "mx, my must be positive");
   const long nx_g = (long)P->p * P->mx + 1, ny_g = (long)P->p * P->my + 1;
@@ -371,7 +474,16 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
     const long node = ((long)(e % P->mx) * P->p + g % n1) + ((long)(e / P->mx) * P->p + g / n1) * nx_g;
     if (node != P->rec_node[r]) return fail(nullptr, SE2GPU_ERR_ARG, "receiver %d: node %d is not GLL point %d of element %d", r, P->rec_node[r], g, e);
   }
-  {
+  // where the device reads pageable host memory, the FP32 modes check the mass in the
+  // kernel that forms 1/M from it (no host pass over the array); elsewhere the host checks
+  int dev0 = 0, pageable0 = 0;
+  if (cudaGetDevice(&dev0) != cudaSuccess ||
+      cudaDeviceGetAttribute(&pageable0, cudaDevAttrPageableMemoryAccess, dev0) != cudaSuccess) {
+    cudaGetLastError();
+    pageable0 = 0;
+  }
+  const bool mass_on_device = (precision != SE2GPU_FP64) && pageable0;
+  if (!mass_on_device) {
     std::atomic<long> bad(LONG_MAX);   // the first node whose mass is not positive and finite
     host_parallel(nnodes, [&](long i0, long i1) {
       for (long i = i0; i < i1; i++)
@@ -438,38 +550,54 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
       for (int f = 0; f < 3; f++) TRY(dzero(h, &h->f64[b][f], vbytes));
     TRY(upload(h, &h->mass, P->mass, (size_t)nnodes));   // the reference divides by M
   } else {
-    const bool kahan = (precision == SE2GPU_FP32_KAHAN);
+    const bool kahan = is_kahan(h), df = is_df(h);
     h->pitch = (int)((nx_g + 1 + 15) / 16 * 16);   // >= 1 padding node: paired reads stay in the row
     const size_t np = (size_t)ny_g * h->pitch;
     for (int b = 0; b < 2; b++) {
       TRY(dzero(h, (void **)&h->pu[b], np * 8));
       TRY(dzero(h, (void **)&h->pw[b], np * 8));
       if (kahan) { TRY(dzero(h, (void **)&h->pcu[b], np * 8)); TRY(dzero(h, (void **)&h->pcw[b], np * 8)); }
-      TRY(dzero(h, (void **)&h->rbuf[b], (size_t)P->nrec * npe * 6 * 4));
+      TRY(dzero(h, (void **)&h->rbuf[b], (size_t)P->nrec * npe * rbuf_values(h) * 4));
     }
-    TRY(dzero(h, (void **)&h->pa, np * 8));
+    TRY(dzero(h, (void **)&h->pa, np * 8 * (df ? 2 : 1)));   // two-float mode: low parts after the high
     if (h->pageable) {
       // the device reads the mass where it lies (no staging copy of the whole array)
-      TRY(dalloc(h, (void **)&h->pminv, np * 4));
-      k_minv_from_host<<<4 * h->nsm, 256, 0, h->stream>>>(P->mass, nx_g, ny_g, h->pitch, h->pminv);
-      if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(h->stream) != cudaSuccess) {
+      TRY(dalloc(h, (void **)&h->pminv, np * 4 * (df ? 2 : 1)));
+      TRY(dalloc(h, (void **)&h->mass_bad, sizeof(unsigned long long)));
+      if (cudaMemsetAsync(h->mass_bad, 0xff, sizeof(unsigned long long), h->stream) != cudaSuccess) {
+        fail(h, SE2GPU_ERR_CUDA, "mass check set-up");
+        TRY(SE2GPU_ERR_CUDA);
+      }
+      k_minv_from_host<<<4 * h->nsm, 256, 0, h->stream>>>(P->mass, nx_g, ny_g, h->pitch, h->pminv,
+                                                          df ? h->pminv + np : nullptr, h->mass_bad);
+      if (cudaGetLastError() != cudaSuccess) {
         fail(h, SE2GPU_ERR_CUDA, "1/M from host memory");
         TRY(SE2GPU_ERR_CUDA);
       }
     } else {
-      // 1/M in the padded FP32 layout (padding nodes 0), row blocks on the host threads
-      std::unique_ptr<float[]> minv(new float[np]);
+      // 1/M in the padded FP32 layout (padding nodes 0), row blocks on the host threads;
+      // the two-float mode appends the remainders
+      const size_t nm = np * (df ? 2 : 1);
+      std::unique_ptr<float[]> minv(new float[nm]);
       const int pitch = h->pitch;
       host_parallel(ny_g, [&](long y0, long y1) {
         for (long y = y0; y < y1; y++) {
           float *row = minv.get() + (size_t)y * pitch;
+          float *lo = df ? row + np : nullptr;
           const double *m = P->mass + y * nx_g;
-          for (long x = 0; x < nx_g; x++) row[x] = (float)(1.0 / m[x]);
-          for (long x = nx_g; x < pitch; x++) row[x] = 0.f;
+          for (long x = 0; x < nx_g; x++) {
+            const double r = 1.0 / m[x];
+            row[x] = (float)r;
+            if (lo) lo[x] = (float)(r - (double)row[x]);
+          }
+          for (long x = nx_g; x < pitch; x++) {
+            row[x] = 0.f;
+            if (lo) lo[x] = 0.f;
+          }
         }
       });
-      TRY(dalloc(h, (void **)&h->pminv, np * 4));
-      if (cudaMemcpy(h->pminv, minv.get(), np * 4, cudaMemcpyHostToDevice) != cudaSuccess) { fail(h, SE2GPU_ERR_CUDA, "upload 1/M"); TRY(SE2GPU_ERR_CUDA); }
+      TRY(dalloc(h, (void **)&h->pminv, nm * 4));
+      if (cudaMemcpyAsync(h->pminv, minv.get(), nm * 4, cudaMemcpyHostToDevice, h->stream) != cudaSuccess) { fail(h, SE2GPU_ERR_CUDA, "upload 1/M"); TRY(SE2GPU_ERR_CUDA); }
     }
     {
       cudaError_t e = se2p::set_tables(P->p, P->D, P->w1d);
@@ -477,6 +605,23 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
       h->src_elem_h = new std::vector<int>(P->src_elem, P->src_elem + P->nsrc);
       h->rec_elem_h = new std::vector<int>(P->rec_elem, P->rec_elem + P->nrec);
       TRY(setup_f32_config(h, 0));
+    }
+  }
+  {
+    // one wait for everything queued above (kernels that read the caller's arrays included),
+    // then the device's mass check
+    unsigned long long bad = ~0ULL;
+    cudaError_t e = h->mass_bad ? cudaMemcpyAsync(&bad, h->mass_bad, sizeof(bad), cudaMemcpyDeviceToHost, h->stream)
+                                : cudaSuccess;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      fail(h, SE2GPU_ERR_CUDA, "set-up: %s", cudaGetErrorString(e));
+      TRY(SE2GPU_ERR_CUDA);
+    }
+    if (bad != ~0ULL) {
+      fail(h, SE2GPU_ERR_ARG, "mass at node %ld is not positive", (long)bad);
+      TRY(SE2GPU_ERR_ARG);
     }
   }
 #undef TRY
@@ -495,7 +640,7 @@ extern "C" int se2gpu_set_stream(se2gpu_solver *h, void *stream)
 static int check_err_flag(se2gpu_solver *h)
 {
   int flag = 0;
-  CK(h, cudaMemcpy(&flag, h->err_dev, sizeof(int), cudaMemcpyDeviceToHost));
+  CK(h, cudaMemcpyAsync(&flag, h->err_dev, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   if (flag) return fail(h, SE2GPU_ERR_CUDA, "a step kernel gave up waiting for its tile copies (bounded wait expired)");
   return 0;
 }
@@ -559,6 +704,7 @@ static se2p::Params f32_params(se2gpu_solver *h)
   prm.J00 = (const float *)h->J00; prm.J11 = (const float *)h->J11;
   prm.iJ00 = (const float *)h->iJ00; prm.iJ11 = (const float *)h->iJ11;
   prm.dt = (float)h->dt; prm.half_dt = (float)(0.5 * h->dt);
+  prm.dt_lo = (float)(h->dt - (double)prm.dt); prm.half_dt_lo = (float)(0.5 * h->dt - (double)prm.half_dt);
   prm.nsrc = h->nsrc; prm.src_elem = h->src_elem; prm.src_vals = (const float *)h->src_vals;
   prm.nrec = h->nrec; prm.rec_elem = h->rec_elem; prm.rec_gll = h->rec_gll;
   prm.Dd = h->Dd; prm.iJ00d = h->iJ00d; prm.iJ11d = h->iJ11d;
@@ -588,7 +734,7 @@ static int flush_record(se2gpu_solver *h)
     prm.rbuf_in = h->rbuf[h->rlast];
     prm.record = 1;
     prm.trace_row = row;
-    e = se2p::launch_record(h->p, prm, h->stream);
+    e = se2p::launch_record(h->p, prm, h->stream, is_df(h));
   }
   if (e != cudaSuccess) return fail(h, SE2GPU_ERR_CUDA, "receiver kernel: %s", cudaGetErrorString(e));
   h->rows_written++;
@@ -618,7 +764,7 @@ static int advance_f64(se2gpu_solver *h, int nsteps)
 static int advance_f32(se2gpu_solver *h, int nsteps)
 {
   auto prm = f32_params(h);
-  const bool kahan = is_kahan(h);
+  const int mode = pmode(h);
   for (int k = 0; k < nsteps; k++) {
     const int in = h->cur, outb = 1 - h->cur;
     prm.u_out = h->pu[outb]; prm.w_out = h->pw[outb]; prm.cu_out = h->pcu[outb]; prm.cw_out = h->pcw[outb];
@@ -629,7 +775,7 @@ static int advance_f32(se2gpu_solver *h, int nsteps)
     prm.record = h->pending_record ? 1 : 0;
     prm.trace_row = h->traces + (size_t)h->rows_written * 7 * h->nrec;
     h->launches++;
-    cudaError_t e = se2p::launch_step(h->p, h->pconfig, kahan, h->maps[in], prm, h->pgrid, h->stream);
+    cudaError_t e = se2p::launch_step(h->p, h->pconfig, mode, h->maps[in], prm, h->pgrid, h->stream);
     if (e != cudaSuccess) return fail(h, SE2GPU_ERR_CUDA, "step kernel: %s", cudaGetErrorString(e));
     if (h->pending_record) { h->rows_written++; h->pending_record = false; }
     h->cur = outb;
@@ -652,7 +798,7 @@ extern "C" int se2gpu_advance(se2gpu_solver *h, int nsteps, const double *stf)
   if (h->nsrc) {
     if (nsteps > h->stf_cap) {
       CK(h, cudaStreamSynchronize(h->stream));
-      cudaFree(h->stf_dev);
+      dfree(h, h->stf_dev);
       h->stf_dev = nullptr;
       int rc = dalloc(h, (void **)&h->stf_dev, (size_t)nsteps * h->nsrc * 8);
       if (rc) { h->stf_cap = 0; return rc; }
@@ -728,22 +874,24 @@ extern "C" int se2gpu_get_fields(se2gpu_solver *h, double *u, double *v, double 
     prefault_output(v, n);
     prefault_output(a, n);
     k_fields_to_host<<<4 * h->nsm, 256, 0, h->stream>>>(h->pu[c], h->pw[c], kahan ? h->pcu[c] : nullptr,
-                                                        kahan ? h->pcw[c] : nullptr, h->pa, h->nx_g, h->ny_g, h->pitch,
+                                                        kahan ? h->pcw[c] : nullptr, h->pa, pa_lo(h), h->nx_g, h->ny_g, h->pitch,
                                                         h->dt, 0.5 * h->dt, u, v, a);
     CK(h, cudaGetLastError());
     CK(h, cudaStreamSynchronize(h->stream));
     return 0;
   }
   const size_t np = (size_t)h->ny_g * h->pitch;
-  std::vector<float2> U(np), W(np), CU(np, make_float2(0.f, 0.f)), CW(np, make_float2(0.f, 0.f)), A(np);
+  std::vector<float2> U(np), W(np), CU(np, make_float2(0.f, 0.f)), CW(np, make_float2(0.f, 0.f)), A(np),
+      AL(np, make_float2(0.f, 0.f));
   const int c = h->cur;
-  CK(h, cudaMemcpy(U.data(), h->pu[c], np * 8, cudaMemcpyDeviceToHost));
-  CK(h, cudaMemcpy(W.data(), h->pw[c], np * 8, cudaMemcpyDeviceToHost));
+  CK(h, cudaMemcpyAsync(U.data(), h->pu[c], np * 8, cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaMemcpyAsync(W.data(), h->pw[c], np * 8, cudaMemcpyDeviceToHost, h->stream));
   if (is_kahan(h)) {
-    CK(h, cudaMemcpy(CU.data(), h->pcu[c], np * 8, cudaMemcpyDeviceToHost));
-    CK(h, cudaMemcpy(CW.data(), h->pcw[c], np * 8, cudaMemcpyDeviceToHost));
+    CK(h, cudaMemcpyAsync(CU.data(), h->pcu[c], np * 8, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemcpyAsync(CW.data(), h->pcw[c], np * 8, cudaMemcpyDeviceToHost, h->stream));
   }
-  CK(h, cudaMemcpy(A.data(), h->pa, np * 8, cudaMemcpyDeviceToHost));
+  CK(h, cudaMemcpyAsync(A.data(), h->pa, np * 8, cudaMemcpyDeviceToHost, h->stream));
+  if (pa_lo(h)) CK(h, cudaMemcpyAsync(AL.data(), pa_lo(h), np * 8, cudaMemcpyDeviceToHost, h->stream));
   const double dt = h->dt, hdt = 0.5 * h->dt;
   for (long y = 0; y < h->ny_g; y++)
     for (long x = 0; x < h->nx_g; x++) {
@@ -751,8 +899,9 @@ extern "C" int se2gpu_get_fields(se2gpu_solver *h, double *u, double *v, double 
       const double w0 = (double)W[k].x - (double)CW[k].x, w1 = (double)W[k].y - (double)CW[k].y;
       const double u0 = (double)U[k].x - (double)CU[k].x, u1 = (double)U[k].y - (double)CU[k].y;
       if (u) { u[2 * nn] = u0 - dt * w0; u[2 * nn + 1] = u1 - dt * w1; }
-      if (v) { v[2 * nn] = w0 - hdt * (double)A[k].x; v[2 * nn + 1] = w1 - hdt * (double)A[k].y; }
-      if (a) { a[2 * nn] = (double)A[k].x; a[2 * nn + 1] = (double)A[k].y; }
+      const double a0 = (double)A[k].x + (double)AL[k].x, a1 = (double)A[k].y + (double)AL[k].y;
+      if (v) { v[2 * nn] = w0 - hdt * a0; v[2 * nn + 1] = w1 - hdt * a1; }
+      if (a) { a[2 * nn] = a0; a[2 * nn + 1] = a1; }
     }
   return 0;
 }
@@ -769,7 +918,7 @@ extern "C" int se2gpu_norms(se2gpu_solver *h, double out[6])
     CK(h, cudaGetLastError());
   } else {
     CK(h, se2p::launch_norms(h->pu[h->cur], h->pw[h->cur], is_kahan(h) ? h->pcu[h->cur] : nullptr,
-                             is_kahan(h) ? h->pcw[h->cur] : nullptr, h->pa, h->nx_g, h->ny_g, h->pitch, h->dt,
+                             is_kahan(h) ? h->pcw[h->cur] : nullptr, h->pa, pa_lo(h), h->nx_g, h->ny_g, h->pitch, h->dt,
                              h->norm_part, nb, h->stream));
   }
   std::vector<double> part(6 * nb);
@@ -827,19 +976,19 @@ extern "C" int se2gpu_assemble_linear_form(se2gpu_solver *h, const double *u, do
   if (!h->scratch_f && (rc = dalloc(h, &h->scratch_f, n * h->tsize))) return rc;
   CK(h, cudaStreamSynchronize(h->stream));
   if (h->tsize == 8) {
-    CK(h, cudaMemcpy(h->scratch_u, u, n * 8, cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpyAsync(h->scratch_u, u, n * 8, cudaMemcpyHostToDevice, h->stream));
   } else {
     std::vector<float> tmp(n);
     for (size_t i = 0; i < n; i++) tmp[i] = (float)u[i];
-    CK(h, cudaMemcpy(h->scratch_u, tmp.data(), n * 4, cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpyAsync(h->scratch_u, tmp.data(), n * 4, cudaMemcpyHostToDevice, h->stream));
   }
   if ((rc = se2gpu_assemble_linear_form_device(h, h->scratch_u, h->scratch_f))) return rc;
   CK(h, cudaStreamSynchronize(h->stream));
   if (h->tsize == 8) {
-    CK(h, cudaMemcpy(F, h->scratch_f, n * 8, cudaMemcpyDeviceToHost));
+    CK(h, cudaMemcpyAsync(F, h->scratch_f, n * 8, cudaMemcpyDeviceToHost, h->stream));
   } else {
     std::vector<float> tmp(n);
-    CK(h, cudaMemcpy(tmp.data(), h->scratch_f, n * 4, cudaMemcpyDeviceToHost));
+    CK(h, cudaMemcpyAsync(tmp.data(), h->scratch_f, n * 4, cudaMemcpyDeviceToHost, h->stream));
     for (size_t i = 0; i < n; i++) F[i] = (double)tmp[i];
   }
   return 0;
@@ -879,7 +1028,7 @@ extern "C" int se2gpu_tile_configs(const se2gpu_solver *h, int *edge, int *threa
   const int n = se2p::num_configs(h->p);
   for (int c = 0; c < n && c < max_configs; c++) {
     se2p::TileShape ts;
-    se2p::config_shape(h->p, c, is_kahan(h), &ts);
+    se2p::config_shape(h->p, c, pmode(h), &ts);
     if (edge) edge[c] = ts.tex;
     if (threads) threads[c] = ts.nt;
   }
@@ -895,14 +1044,14 @@ extern "C" int se2gpu_tile_config_info(const se2gpu_solver *h, int config, int i
     return 0;
   }
   se2p::TileShape ts;
-  if (config < 0 || se2p::config_shape(h->p, config, is_kahan(h), &ts)) return SE2GPU_ERR_ARG;
+  if (config < 0 || se2p::config_shape(h->p, config, pmode(h), &ts)) return SE2GPU_ERR_ARG;
   info[0] = ts.tex; info[1] = ts.nt; info[2] = ts.owned_buffers;
   // the occupancy query needs the kernel's dynamic shared-memory limit raised first
-  if (cudaSetDevice(h->device) != cudaSuccess || se2p::prepare(h->p, config, is_kahan(h)) != cudaSuccess) {
+  if (cudaSetDevice(h->device) != cudaSuccess || se2p::prepare(h->p, config, pmode(h)) != cudaSuccess) {
     cudaGetLastError();
     return SE2GPU_ERR_CUDA;
   }
-  info[3] = se2p::occupancy(h->p, config, is_kahan(h), false);
+  info[3] = se2p::occupancy(h->p, config, pmode(h), false);
   return 0;
 }
 
@@ -936,8 +1085,8 @@ std::vector<std::pair<void *, size_t>> state_arrays(se2gpu_solver *h)
     v.push_back({h->pu[h->cur], b});
     v.push_back({h->pw[h->cur], b});
     if (is_kahan(h)) { v.push_back({h->pcu[h->cur], b}); v.push_back({h->pcw[h->cur], b}); }
-    v.push_back({h->pa, b});
-    if (h->nrec) v.push_back({h->rbuf[h->rlast], (size_t)h->nrec * h->npe * 6 * 4});
+    v.push_back({h->pa, b * (is_df(h) ? 2 : 1)});
+    if (h->nrec) v.push_back({h->rbuf[h->rlast], (size_t)h->nrec * h->npe * rbuf_values(h) * 4});
   }
   return v;
 }
@@ -969,7 +1118,7 @@ extern "C" int se2gpu_checkpoint_save(se2gpu_solver *h, void *buf, long bytes)
   memcpy(o, &hd, sizeof(hd));
   o += sizeof(hd);
   for (auto &a : state_arrays(h)) {
-    CK(h, cudaMemcpy(o, a.first, a.second, cudaMemcpyDeviceToHost));
+    CK(h, cudaMemcpyAsync(o, a.first, a.second, cudaMemcpyDeviceToHost, h->stream));
     o += a.second;
   }
   return 0;
@@ -995,7 +1144,7 @@ extern "C" int se2gpu_checkpoint_load(se2gpu_solver *h, const void *buf, long by
   if (!is_f64(h)) h->rlast = hd.rlast & 1;
   const char *o = static_cast<const char *>(buf) + sizeof(hd);
   for (auto &a : state_arrays(h)) {
-    CK(h, cudaMemcpy(a.first, o, a.second, cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpyAsync(a.first, o, a.second, cudaMemcpyHostToDevice, h->stream));
     o += a.second;
   }
   return 0;

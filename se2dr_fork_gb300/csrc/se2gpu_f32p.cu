@@ -1,6 +1,6 @@
-// se2gpu_f32p.cu -- persistent TMA-pipelined FP32 kernels (plain / Kahan), degrees 1..8,
-// the tile configurations the autotuner chooses from, and their host-side helpers
-// (tensor maps, constant tables, norms of the leapfrog state).
+// se2gpu_f32p.cu -- persistent TMA-pipelined FP32 kernels (plain / Kahan; the two-float mode is
+// in se2gpu_f32df.cu), degrees 1..8, the tile configurations the autotuner chooses from, and
+// their host-side helpers (tensor maps, constant tables, norms of the leapfrog state).
 #include <cudaTypedefs.h>
 
 #include "se2gpu_persist.cuh"
@@ -16,7 +16,9 @@ cudaError_t set_tables(int p, const double *D, const double *w1d)
   for (int i = 0; i < n1; i++) w[i] = (float)w1d[i];
   cudaError_t e = cudaMemcpyToSymbol(c_D, d, sizeof(d), sizeof(d) * (p - 1));
   if (e != cudaSuccess) return e;
-  return cudaMemcpyToSymbol(c_w, w, sizeof(w), sizeof(w) * (p - 1));
+  e = cudaMemcpyToSymbol(c_w, w, sizeof(w), sizeof(w) * (p - 1));
+  if (e != cudaSuccess) return e;
+  return df_set_tables(p, D, w1d);
 }
 
 // ---- one configuration = (degree, elements per tile edge, threads) ----------
@@ -48,23 +50,11 @@ static Entry entry()
   return e;
 }
 
-// every (element, line) item of a tile gets its own thread: NT >= (TE+1)^2 (P+1).
-// entry<P, TE, NT, owned buffers, CTAs per SM the registers are sized for (0: as many
-// as the shared memory allows, up to 3)>
 static const Entry *table(int *n)
 {
-  static Entry t[] = {
-      entry<1, 15, 512>(), entry<1, 11, 288>(),
-      entry<2, 12, 512, 2, 2>(), entry<2, 10, 384>(), entry<2, 8, 256>(),
-      entry<3, 7, 256>(),  entry<3, 8, 352>(),
-      // degree 4: 7x7 with one owned buffer kept at 2 CTAs per SM (92 registers) is the
-      // fastest; sized for 3 CTAs it is capped at 64 registers and runs slower
-      entry<4, 7, 320, 1, 2>(), entry<4, 7, 320, 2>(), entry<4, 6, 256, 2>(), entry<4, 8, 416>(),
-      entry<5, 6, 320>(),  entry<5, 5, 224>(),
-      entry<6, 5, 256>(),  entry<6, 4, 192>(),
-      entry<7, 4, 224>(),  entry<7, 5, 288>(),
-      entry<8, 4, 256>(),  entry<8, 3, 160>(),
-  };
+#define SE2P_ENTRY(P, TE, NT, NOB, MINB) entry<P, TE, NT, (NOB) ? (NOB) : owned_buffers(P), MINB>(),
+  static Entry t[] = {SE2P_CONFIGS(SE2P_ENTRY)};
+#undef SE2P_ENTRY
   *n = (int)(sizeof(t) / sizeof(t[0]));
   return t;
 }
@@ -89,28 +79,33 @@ int num_configs(int p)
   return k;
 }
 
-int config_shape(int p, int config, bool kahan, TileShape *s)
+int config_shape(int p, int config, int mode, TileShape *s)
 {
   const Entry *e = find(p, config);
   if (!e) return -1;
+  size_t df_smem = 0;
+  if (mode == MODE_DF && !df_kernel(p, config, &df_smem)) return -1;
   s->tex = s->tey = e->te;
   s->nt = e->nt;
   s->region_w = round_up((e->te + 1) * p + 2 + ((p & 1) ? 2 : 0), 2);
   s->region_h = (e->te + 1) * p + 1;
   s->own_w = round_up(e->te * p + 2, 2);
   s->own_h = e->te * p + 1;
-  s->owned_buffers = e->nob;
-  s->smem = e->smem[kahan ? 1 : 0];
+  s->owned_buffers = (mode == MODE_DF) ? 1 : e->nob;
+  s->smem = (mode == MODE_DF) ? df_smem : e->smem[mode ? 1 : 0];
   return 0;
 }
 
-cudaError_t prepare(int p, int config, bool kahan)
+cudaError_t prepare(int p, int config, int mode)
 {
   const Entry *e = find(p, config);
   if (!e) return cudaErrorInvalidValue;
-  const int k = kahan ? 1 : 0;
-  const void *fns[2] = {e->fn[k], e->bfn[k]};
-  const size_t sizes[2] = {e->smem[k], e->bsmem[k]};
+  const int k = mode ? 1 : 0;
+  size_t df_smem = 0;
+  const void *dfn = (mode == MODE_DF) ? df_kernel(p, config, &df_smem) : nullptr;
+  if (mode == MODE_DF && !dfn) return cudaErrorInvalidValue;
+  const void *fns[2] = {dfn ? dfn : e->fn[k], e->bfn[k]};
+  const size_t sizes[2] = {dfn ? df_smem : e->smem[k], e->bsmem[k]};
   for (int i = 0; i < 2; i++) {
     const void *fn = fns[i];
     cudaError_t r = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizes[i]);
@@ -121,27 +116,35 @@ cudaError_t prepare(int p, int config, bool kahan)
   return cudaSuccess;
 }
 
-int occupancy(int p, int config, bool kahan, bool batch)
+int occupancy(int p, int config, int mode, bool batch)
 {
   const Entry *e = find(p, config);
   int n = 0;
-  if (!e || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, (batch ? e->bfn : e->fn)[kahan ? 1 : 0], e->nt,
-                                                          (batch ? e->bsmem : e->smem)[kahan ? 1 : 0]) != cudaSuccess) {
+  if (!e) return 1;
+  const int k = mode ? 1 : 0;
+  const void *fn = (batch ? e->bfn : e->fn)[k];
+  size_t smem = (batch ? e->bsmem : e->smem)[k];
+  if (mode == MODE_DF && !batch) fn = df_kernel(p, config, &smem);
+  if (!fn || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, e->nt, smem) != cudaSuccess) {
     cudaGetLastError();
     return 1;
   }
   return n;
 }
 
-cudaError_t launch_step(int p, int config, bool kahan, const CUtensorMap *maps, const Params &prm, int grid,
+cudaError_t launch_step(int p, int config, int mode, const CUtensorMap *maps, const Params &prm, int grid,
                         cudaStream_t st)
 {
   const Entry *e = find(p, config);
   if (!e) return cudaErrorInvalidValue;
+  const void *fn = e->fn[mode ? 1 : 0];
+  size_t smem = e->smem[mode ? 1 : 0];
+  if (mode == MODE_DF) fn = df_kernel(p, config, &smem);
+  if (!fn) return cudaErrorInvalidValue;
   Params pc = prm;
   CUtensorMap m0 = maps[0], m1 = maps[1], m2 = maps[2], m3 = maps[3];
   void *args[] = {&m0, &m1, &m2, &m3, &pc};
-  return cudaLaunchKernel(e->fn[kahan ? 1 : 0], dim3(grid), dim3(e->nt), args, e->smem[kahan ? 1 : 0], st);
+  return cudaLaunchKernel(fn, dim3(grid), dim3(e->nt), args, smem, st);
 }
 
 cudaError_t launch_batch(int p, int config, bool kahan, const BatchArgs &ba, int grid, cudaStream_t st)
@@ -177,8 +180,9 @@ static cudaError_t record_t(const Params &prm, cudaStream_t st)
   persist_record<P><<<1, 128, 0, st>>>(prm);
   return cudaGetLastError();
 }
-cudaError_t launch_record(int p, const Params &prm, cudaStream_t st)
+cudaError_t launch_record(int p, const Params &prm, cudaStream_t st, bool df)
 {
+  if (df) return df_launch_record(p, prm, st);
   switch (p) {
     case 1: return record_t<1>(prm, st); case 2: return record_t<2>(prm, st);
     case 3: return record_t<3>(prm, st); case 4: return record_t<4>(prm, st);
@@ -214,18 +218,18 @@ int make_map(CUtensorMap *map, void *base, int nx, int ny, int pitch, int bw, in
 // norms of (u_k, v_k) recovered from the leapfrog state in FP64:
 // u_k = (u - cu) - dt (w - cw),  v_k = (w - cw) - dt/2 a_k
 __global__ void norms_leapfrog(const float2 *u, const float2 *w, const float2 *cu, const float2 *cw, const float2 *a,
-                               int nx, int ny, int pitch, double dt, double half_dt, double *part)
+                               const float2 *al, int nx, int ny, int pitch, double dt, double half_dt, double *part)
 {
   __shared__ double s[6][256];
   double umax = -1.0e308, umin = 1.0e308, uss = 0.0, vmax = -1.0e308, vmin = 1.0e308, vss = 0.0;
   const long n = (long)nx * ny;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const long y = i / nx, x = i - y * nx, k = y * pitch + x;
-    const float2 uu = u[k], ww = w[k], aa = a[k];
+    const float2 uu = u[k], ww = w[k], aa = a[k], aal = al ? al[k] : make_float2(0.f, 0.f);
     const float2 cuu = cu ? cu[k] : make_float2(0.f, 0.f), cww = cw ? cw[k] : make_float2(0.f, 0.f);
     const double wx = (double)ww.x - (double)cww.x, wy = (double)ww.y - (double)cww.y;
     const double ux = ((double)uu.x - (double)cuu.x) - dt * wx, uy = ((double)uu.y - (double)cuu.y) - dt * wy;
-    const double vx = wx - half_dt * (double)aa.x, vy = wy - half_dt * (double)aa.y;
+    const double vx = wx - half_dt * ((double)aa.x + (double)aal.x), vy = wy - half_dt * ((double)aa.y + (double)aal.y);
     umax = fmax(umax, fmax(ux, uy)); umin = fmin(umin, fmin(ux, uy)); uss += ux * ux + uy * uy;
     vmax = fmax(vmax, fmax(vx, vy)); vmin = fmin(vmin, fmin(vx, vy)); vss += vx * vx + vy * vy;
   }
@@ -243,10 +247,11 @@ __global__ void norms_leapfrog(const float2 *u, const float2 *w, const float2 *c
   if (threadIdx.x < 6) part[blockIdx.x * 6 + threadIdx.x] = s[threadIdx.x][0];
 }
 
-cudaError_t launch_norms(const float2 *u, const float2 *w, const float2 *cu, const float2 *cw, const float2 *a, int nx,
-                         int ny, int pitch, double dt, double *part, int nblocks, cudaStream_t st)
+cudaError_t launch_norms(const float2 *u, const float2 *w, const float2 *cu, const float2 *cw, const float2 *a,
+                         const float2 *al, int nx, int ny, int pitch, double dt, double *part, int nblocks,
+                         cudaStream_t st)
 {
-  norms_leapfrog<<<nblocks, 256, 0, st>>>(u, w, cu, cw, a, nx, ny, pitch, dt, 0.5 * dt, part);
+  norms_leapfrog<<<nblocks, 256, 0, st>>>(u, w, cu, cw, a, al, nx, ny, pitch, dt, 0.5 * dt, part);
   return cudaGetLastError();
 }
 

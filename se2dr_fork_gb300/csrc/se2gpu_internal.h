@@ -27,6 +27,7 @@ struct se2gpu_solver {
   int pitch;
   float2 *pu[2], *pw[2], *pcu[2], *pcw[2], *pa;
   float *pminv, *rbuf[2];
+  unsigned long long *mass_bad;  // first node with a mass that is not positive (device check at create)
   int rlast;
   CUtensorMap maps[2][4];
   int pgrid, pconfig, pntx, pnty;

@@ -50,6 +50,9 @@ namespace se2p {
 // into one translation unit only)
 __constant__ float c_D[8][81];
 __constant__ float c_w[8][9];
+// their low parts (FP64 value - FP32 value, rounded to FP32) for the two-float mode
+__constant__ float c_Dl[8][81];
+__constant__ float c_wl[8][9];
 
 // ---------------------------------------------------------------- PTX helpers
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -134,7 +137,7 @@ __host__ __device__ constexpr size_t al128(size_t x) { return (x + 127) & ~size_
 // there, and at degree 8 it fits 2 CTAs per SM instead of 1)
 __host__ __device__ constexpr int owned_buffers(int p) { return p <= 3 ? 2 : 1; }
 
-template <int P, int TE, bool KAHAN, int NOB = owned_buffers(P)>
+template <int P, int TE, bool KAHAN, int NOB = owned_buffers(P), bool DF = false>
 struct Layout {
   typedef Geo<P, TE> G;
   static constexpr size_t REG = al128(sizeof(float2) * G::BXW * G::BXH);
@@ -144,7 +147,8 @@ struct Layout {
   // NOB = 2 buffers hold this tile's and the next's, NOB = 1 this tile's only.
   static constexpr size_t STAGE = REG * (KAHAN ? 2 : 1);
   static constexpr size_t OWNB = OWN * (KAHAN ? 2 : 1);
-  static constexpr size_t XCH = al128(sizeof(float2) * G::NE * G::XS);    // exchange buffer
+  // exchange buffer: float2 per point, float4 (two-float x, y) in the two-float mode
+  static constexpr size_t XCH = al128(sizeof(float2) * (DF ? 2 : 1) * G::NE * G::XS);
   static constexpr size_t MISC = 64;
   static constexpr size_t TOTAL = 2 * STAGE + NOB * OWNB + 2 * XCH + MISC;
   static constexpr size_t BATCH_TOTAL = TOTAL;   // the batched kernel's shot parameters are a kernel parameter
@@ -234,21 +238,23 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float inc)
 }
 
 // receiver rows of the previous step from the side buffer (u, v, a per element node)
-template <int P>
+// (two-float mode: 12 values per node, the value being high + low)
+template <int P, bool DF = false>
 __device__ void sample_rows(const Params &prm, const float *rbuf_in, double *trace_row)
 {
-  constexpr int N1 = P + 1, NPE = N1 * N1;
+  constexpr int N1 = P + 1, NPE = N1 * N1, NV = DF ? 12 : 6;
   for (int r = threadIdx.x; r < prm.nrec; r += blockDim.x) {
-    const float *rb = rbuf_in + (size_t)r * NPE * 6;
+    const float *rb = rbuf_in + (size_t)r * NPE * NV;
+    auto val = [&](int node, int c) { return DF ? (double)rb[node * NV + c] + (double)rb[node * NV + 6 + c] : (double)rb[node * NV + c]; };
     const int g = prm.rec_gll[r], eid = prm.rec_elem[r];
     const int ga = g % N1, gb = g / N1, ex = eid % prm.mx, ey = eid / prm.mx;
     double *o = trace_row + 7 * r;
-    for (int c = 0; c < 6; c++) o[c] = (double)rb[g * 6 + c];
+    for (int c = 0; c < 6; c++) o[c] = val(g, c);
     const double ix = prm.iJ00d[ex], iy = prm.iJ11d[ey];
     double dvxdy = 0.0, dvydx = 0.0;
     for (int k = 0; k < N1; k++) {
-      dvxdy += (iy * prm.Dd[gb * N1 + k]) * (double)rb[(ga + k * N1) * 6 + 2];
-      dvydx += (ix * prm.Dd[ga * N1 + k]) * (double)rb[(k + gb * N1) * 6 + 3];
+      dvxdy += (iy * prm.Dd[gb * N1 + k]) * val(ga + k * N1, 2);
+      dvydx += (ix * prm.Dd[ga * N1 + k]) * val(k + gb * N1, 3);
     }
     o[6] = dvydx - dvxdy;
   }
@@ -577,18 +583,307 @@ __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp,
   return true;
 }
 
+// ---------------------------------------------------------------- two-float arithmetic
+// The two-float mode carries every quantity of a step as an unevaluated sum h + l of
+// two floats (about 48 significant bits).  The building blocks are the error-free
+// transformations TwoSum (Knuth), FastTwoSum (Dekker) and TwoProduct through a fused
+// multiply-add; sums of products are accumulated as in the compensated dot product
+// Dot2 of Ogita, Rump and Oishi (SIAM J. Sci. Comput. 26, 2005): the running sum in h,
+// the errors of every product and addition collected in l, normalised once at the end.
+// Every operation is an explicit round-to-nearest intrinsic, so the compiler neither
+// fuses nor reorders them.
+struct tf {
+  float h, l;
+};
+
+__device__ __forceinline__ tf tf_two_sum(float a, float b)
+{
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return tf{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+// |a| >= |b| (or a == 0)
+__device__ __forceinline__ tf tf_fast_sum(float a, float b)
+{
+  const float s = __fadd_rn(a, b);
+  return tf{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ tf tf_add(tf a, tf b)
+{
+  const tf s = tf_two_sum(a.h, b.h);
+  return tf_fast_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ tf tf_mul(tf a, tf b)
+{
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return tf_fast_sum(p, e);
+}
+__device__ __forceinline__ tf tf_neg(tf a) { return tf{-a.h, -a.l}; }
+// s += a * x, unnormalised (Dot2 step); finish with tf_norm
+__device__ __forceinline__ void tf_dot(tf &s, float ah, float al, tf x)
+{
+  const float p = __fmul_rn(ah, x.h);
+  float e = __fmaf_rn(ah, x.h, -p);
+  e = __fmaf_rn(ah, x.l, e);
+  e = __fmaf_rn(al, x.h, e);
+  const tf t = tf_two_sum(s.h, p);
+  s.h = t.h;
+  s.l = __fadd_rn(s.l, __fadd_rn(t.l, e));
+}
+__device__ __forceinline__ tf tf_norm(tf s) { return tf_two_sum(s.h, s.l); }
+// a double split into its nearest float and the float nearest the remainder
+__device__ __forceinline__ tf tf_from_double(double v)
+{
+  const float h = __double2float_rn(v);
+  return tf{h, __double2float_rn(__dsub_rn(v, (double)h))};
+}
+
+// One tile in the two-float mode: the same phases, items and shared-memory traffic
+// pattern as tile_body, with every value a two-float pair (exchange buffers hold
+// float4 = (x.h, y.h, x.l, y.l)) and the tables' low parts read beside their high
+// parts.  The state keeps the Kahan mode's storage (value = hi - c), so fields,
+// norms and checkpoints are shared with that mode.
+template <int P, int TE, int NT, bool OWAIT>
+__device__ __forceinline__ bool tile_body_df(const Params &prm, const StepPtrs stp, int tx, int ty, const unsigned char *st,
+                                             uint32_t bar, uint32_t parity, const unsigned char *ob, uint32_t bar_o,
+                                             uint32_t par_o, float4 *X1, float4 *X2, int item, int el, int j, int ecx,
+                                             int ecy)
+{
+  typedef Geo<P, TE> G;
+  typedef Layout<P, TE, true, 1, true> L;
+  constexpr int N1 = G::N1, NPE = G::NPE, NEX = G::NEX, BXW = G::BXW, OBW = G::OBW, XS = G::XS;
+  const float *Dh = c_D[P - 1], *Dl = c_Dl[P - 1];
+  const TileBox b = tile_box<P, TE>(prm, tx, ty);
+  const int t = ty * prm.ntx + tx;
+  const int xoff = b.EX0 * P - b.RXa;
+  const bool active = (item < G::ITEMS) && (ecx < b.NEXa) && (ecy < b.NEYa);
+  const int ex = b.EX0 + ecx, ey = b.EY0 + ecy;
+  const size_t ncell = (size_t)prm.mx * prm.my;
+  tf lam{0.f, 0.f}, mu{0.f, 0.f}, ix{0.f, 0.f}, iy{0.f, 0.f}, detJ{0.f, 0.f};
+  if (active) {
+    const size_t cell = (size_t)ey * prm.mx + ex;
+    lam = tf{prm.lam[cell], prm.lam[ncell + cell]};
+    mu = tf{prm.mu[cell], prm.mu[ncell + cell]};
+    ix = tf{prm.iJ00[ex], prm.iJ00[prm.mx + ex]};
+    iy = tf{prm.iJ11[ey], prm.iJ11[prm.my + ey]};
+    detJ = tf_mul(tf{prm.J00[ex], prm.J00[prm.mx + ex]}, tf{prm.J11[ey], prm.J11[prm.my + ey]});
+  }
+  const int s0 = prm.tile_src_off[t], s1 = prm.tile_src_off[t + 1];
+  const int r0 = prm.tile_rec_off[t], r1 = prm.tile_rec_off[t + 1];
+  // node phase: single nodes strided by NT; 1/M (both parts) loaded before the wait
+  constexpr int NOWN = G::OWM * G::OWM;
+  constexpr int MAXS = (NOWN + NT - 1) / NT;
+  const float *minv_lo = prm.minv + (size_t)prm.ny_g * prm.pitch;
+  tf minv_s[MAXS];
+#pragma unroll
+  for (int k = 0; k < MAXS; k++) {
+    minv_s[k] = tf{0.f, 0.f};
+    const int o = threadIdx.x + k * NT, oy = o / G::OWM, ox = o - (o / G::OWM) * G::OWM;
+    if (o < NOWN && oy < b.OH && ox < b.OW) {
+      const size_t n = (size_t)(b.Y0 + oy) * prm.pitch + b.X0 + ox;
+      minv_s[k] = tf{prm.minv[n], minv_lo[n]};
+    }
+  }
+  const bool ok = mbar_wait_bounded(bar, parity);
+  if (__syncthreads_or(!ok)) return false;
+  const float2 *rU = reinterpret_cast<const float2 *>(st);
+  const float2 *rCU = reinterpret_cast<const float2 *>(st + L::REG);
+  const float2 *oW = reinterpret_cast<const float2 *>(ob);
+  const float2 *oCW = reinterpret_cast<const float2 *>(ob + L::OWN);
+
+  // ---- 1. derivatives along row j (registers) and column j (to X1), of the
+  // displacement relative to the line's first node: (u_k - u_0) + (c_0 - c_k) with the
+  // first difference split exactly by TwoSum
+  tf gx[N1], gy[N1];
+  const int base = (ecy * P) * BXW + ecx * P + xoff;
+  if (active) {
+#pragma unroll
+    for (int dir = 0; dir < 2; dir++) {
+      const int stride = dir ? BXW : 1, b0 = dir ? base + j : base + j * BXW;
+      const float2 u0 = rU[b0], c0 = rCU[b0];
+      tf dx[N1], dy[N1];
+#pragma unroll
+      for (int k = 1; k < N1; k++) {
+        const float2 uk = rU[b0 + k * stride], ck = rCU[b0 + k * stride];
+        dx[k] = tf_two_sum(uk.x, -u0.x);
+        dx[k].l = __fsub_rn(dx[k].l, __fsub_rn(ck.x, c0.x));
+        dy[k] = tf_two_sum(uk.y, -u0.y);
+        dy[k].l = __fsub_rn(dy[k].l, __fsub_rn(ck.y, c0.y));
+      }
+#pragma unroll
+      for (int q = 0; q < N1; q++) {
+        tf sx{0.f, 0.f}, sy{0.f, 0.f};
+#pragma unroll
+        for (int k = 1; k < N1; k++) {
+          tf_dot(sx, Dh[q * N1 + k], Dl[q * N1 + k], dx[k]);
+          tf_dot(sy, Dh[q * N1 + k], Dl[q * N1 + k], dy[k]);
+        }
+        sx = tf_norm(sx);
+        sy = tf_norm(sy);
+        if (dir == 0) {
+          gx[q] = sx;
+          gy[q] = sy;
+        } else {
+          X1[el * XS + j + q * N1] = make_float4(sx.h, sy.h, sx.l, sy.l);   // d/deta at (j, q)
+        }
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- 2. stress at the row's points; xi divergence; eta fluxes to X2 ---
+  if (active) {
+    const tf c11 = tf_add(tf_add(mu, mu), lam);
+    const tf nfj = tf_neg(tf_mul(detJ, tf{c_w[P - 1][j], c_wl[P - 1][j]}));
+    tf Fx[N1], Fy[N1];
+#pragma unroll
+    for (int q = 0; q < N1; q++) {
+      const float4 g4 = X1[el * XS + q + j * N1];   // d/deta at (q, j)
+      const tf gex{g4.x, g4.z}, gey{g4.y, g4.w};
+      const tf e0 = tf_mul(ix, gx[q]), e1 = tf_mul(iy, gey);
+      const tf e2 = tf_add(tf_mul(ix, gy[q]), tf_mul(iy, gex));
+      const tf nf = tf_mul(nfj, tf{c_w[P - 1][q], c_wl[P - 1][q]});   // -detJ w_q w_j
+      const tf fx_ = tf_mul(ix, nf), fy_ = tf_mul(iy, nf);
+      const tf sxx = tf_add(tf_mul(c11, e0), tf_mul(lam, e1));
+      const tf syy = tf_add(tf_mul(lam, e0), tf_mul(c11, e1));
+      const tf sxy = tf_mul(mu, e2);
+      Fx[q] = tf_mul(fx_, sxx);
+      Fy[q] = tf_mul(fx_, sxy);
+      const tf hx = tf_mul(fy_, sxy), hy = tf_mul(fy_, syy);
+      X2[el * XS + q + j * N1] = make_float4(hx.h, hy.h, hx.l, hy.l);
+    }
+    // xi part of the divergence for the row's nodes, to X1 (this thread alone read row j of X1)
+#pragma unroll
+    for (int a = 0; a < N1; a++) {
+      tf rx{0.f, 0.f}, ry{0.f, 0.f};
+#pragma unroll
+      for (int q = 0; q < N1; q++) {
+        tf_dot(rx, Dh[q * N1 + a], Dl[q * N1 + a], Fx[q]);
+        tf_dot(ry, Dh[q * N1 + a], Dl[q * N1 + a], Fy[q]);
+      }
+      rx = tf_norm(rx);
+      ry = tf_norm(ry);
+      X1[el * XS + a + j * N1] = make_float4(rx.h, ry.h, rx.l, ry.l);
+    }
+  }
+  __syncthreads();
+
+  // ---- 3. eta part of the divergence along column j, added to X1 -----
+  if (active) {
+    tf fcx[N1], fcy[N1];
+#pragma unroll
+    for (int q = 0; q < N1; q++) {
+      const float4 f4 = X2[el * XS + j + q * N1];
+      fcx[q] = tf{f4.x, f4.z};
+      fcy[q] = tf{f4.y, f4.w};
+    }
+#pragma unroll
+    for (int bq = 0; bq < N1; bq++) {
+      const float4 r = X1[el * XS + j + bq * N1];
+      tf cx{r.x, r.z}, cy{r.y, r.w};
+#pragma unroll
+      for (int q = 0; q < N1; q++) {
+        tf_dot(cx, Dh[q * N1 + bq], Dl[q * N1 + bq], fcx[q]);
+        tf_dot(cy, Dh[q * N1 + bq], Dl[q * N1 + bq], fcy[q]);
+      }
+      cx = tf_norm(cx);
+      cy = tf_norm(cy);
+      X1[el * XS + j + bq * N1] = make_float4(cx.h, cy.h, cx.l, cy.l);
+    }
+  }
+  if (OWAIT) {
+    const bool ok_o = mbar_wait_bounded(bar_o, par_o);
+    if (__syncthreads_or(!ok_o)) return false;
+  } else {
+    __syncthreads();
+  }
+
+  float2 *const u_out = prm.u_out, *const w_out = prm.w_out, *const cu_out = prm.cu_out, *const cw_out = prm.cw_out;
+  float2 *const a_out = stp.a_out;
+  const int pitch = prm.pitch, NXP = prm.mx * P, NYP = prm.my * P;
+  const tf dt{prm.dt, prm.dt_lo}, hdt{prm.half_dt, prm.half_dt_lo};
+  const float *src_lo = prm.src_vals + (size_t)prm.nsrc * 2 * NPE;
+  // ---- owned nodes: ordered element sum, sources, update
+#pragma unroll
+  for (int k = 0; k < MAXS; k++) {
+    const int o = threadIdx.x + k * NT, oy = o / G::OWM, ox = o - (o / G::OWM) * G::OWM;
+    if (o >= NOWN || oy >= b.OH || ox >= b.OW) continue;
+    const int X = b.X0 + ox, Y = b.Y0 + oy;
+    tf fx{0.f, 0.f}, fy{0.f, 0.f};
+    {
+      const int lx = X - b.EX0 * P, ly = Y - b.EY0 * P;
+      const int exl = lx / P, eyl = ly / P, ixl = lx - exl * P, iyl = ly - eyl * P;
+      const bool in_x = X < NXP, in_y = Y < NYP;
+      const bool lft = (ixl == 0) && (X > 0), bot = (iyl == 0) && (Y > 0);
+      const int own = (eyl * NEX + exl) * XS + ixl + iyl * N1;
+      auto add = [&](const float4 fe) {
+        fx = tf_add(fx, tf{fe.x, fe.z});
+        fy = tf_add(fy, tf{fe.y, fe.w});
+      };
+      if (bot && lft) add(X1[own - NEX * XS - XS + P + P * N1]);
+      if (bot && in_x) add(X1[own - NEX * XS + P * N1]);
+      if (lft && in_y) add(X1[own - XS + P]);
+      if (in_x && in_y) add(X1[own]);
+    }
+    for (int q = s0; q < s1; q++) {
+      const int sidx = prm.tile_src_idx[q], se = prm.src_elem[sidx], sx = se % prm.mx, sy = se / prm.mx;
+      const int a = X - sx * P, bb = Y - sy * P;
+      if (a >= 0 && a <= P && bb >= 0 && bb <= P) {
+        const tf val = tf_from_double(stp.stf[sidx]);
+        const size_t vi = (size_t)sidx * 2 * NPE + 2 * (a + bb * N1);
+        fx = tf_add(fx, tf_mul(val, tf{prm.src_vals[vi], src_lo[vi]}));
+        fy = tf_add(fy, tf_mul(val, tf{prm.src_vals[vi + 1], src_lo[vi + 1]}));
+      }
+    }
+    const tf ax = tf_mul(fx, minv_s[k]), ay = tf_mul(fy, minv_s[k]);
+    const int ri = (Y - b.RYa) * BXW + (X - b.RXa);
+    const int oi = oy * OBW + (X - b.OXa);
+    const float2 u = rU[ri], cu = rCU[ri], w = oW[oi], cw = oCW[oi];
+    const tf ux{u.x, -cu.x}, uy{u.y, -cu.y}, wx{w.x, -cw.x}, wy{w.y, -cw.y};
+    for (int q = r0; q < r1; q++) {
+      const int r = prm.tile_rec_idx[q], re = prm.rec_elem[r], rx = re % prm.mx, ry = re / prm.mx;
+      const int a = X - rx * P, bb = Y - ry * P;
+      if (a >= 0 && a <= P && bb >= 0 && bb <= P) {
+        float *rb = stp.rbuf_out + ((size_t)r * NPE + a + bb * N1) * 12;
+        const tf vx = tf_add(wx, tf_mul(hdt, ax)), vy = tf_add(wy, tf_mul(hdt, ay));
+        const tf uxn = tf_norm(ux), uyn = tf_norm(uy);
+        rb[0] = uxn.h; rb[1] = uyn.h; rb[2] = vx.h; rb[3] = vy.h; rb[4] = ax.h; rb[5] = ay.h;
+        rb[6] = uxn.l; rb[7] = uyn.l; rb[8] = vx.l; rb[9] = vy.l; rb[10] = ax.l; rb[11] = ay.l;
+      }
+    }
+    const tf wxn = tf_add(wx, tf_mul(dt, ax)), wyn = tf_add(wy, tf_mul(dt, ay));
+    const tf uxn = tf_add(ux, tf_mul(dt, wxn)), uyn = tf_add(uy, tf_mul(dt, wyn));
+    const size_t n = (size_t)Y * pitch + X;
+    u_out[n] = make_float2(uxn.h, uyn.h);
+    w_out[n] = make_float2(wxn.h, wyn.h);
+    cu_out[n] = make_float2(-uxn.l, -uyn.l);
+    cw_out[n] = make_float2(-wxn.l, -wyn.l);
+    if (a_out) {
+      a_out[n] = make_float2(ax.h, ay.h);
+      a_out[(size_t)prm.ny_g * pitch + n] = make_float2(ax.l, ay.l);   // low parts after the high parts
+    }
+  }
+  __syncthreads();   // stage s, the owned buffer and the exchange buffers are free again
+  return true;
+}
+
+// DF: the two-float mode (KAHAN storage, tile_body_df)
 template <int P, int TE, int NT, bool KAHAN, int NOB = owned_buffers(P),
-          int MINB = min_blocks(Layout<P, TE, KAHAN, NOB>::TOTAL)>
+          int MINB = min_blocks(Layout<P, TE, KAHAN, NOB>::TOTAL), bool DF = false>
 __global__ void __launch_bounds__(NT, MINB)
 persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ CUtensorMap tm_cu,
              const __grid_constant__ CUtensorMap tm_w, const __grid_constant__ CUtensorMap tm_cw,
              const Params prm)
 {
   typedef Geo<P, TE> G;
-  typedef Layout<P, TE, KAHAN, NOB> L;
+  typedef Layout<P, TE, KAHAN, NOB, DF> L;
   constexpr int N1 = G::N1, NEX = G::NEX;
   static_assert(NT >= G::ITEMS, "one (element, line) item per thread");
   static_assert(NOB == 1 || NOB == 2, "one or two owned-box buffers");
+  static_assert(!DF || (KAHAN && NOB == 1), "the two-float mode keeps the Kahan storage and one owned buffer");
   const float *W = c_w[P - 1];
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char *stage0 = smem;
@@ -609,7 +904,7 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
     if (KAHAN) { prefetch_map(&tm_cu); prefetch_map(&tm_cw); }
   }
   __syncthreads();
-  if (blockIdx.x == 0 && prm.record) sample_rows<P>(prm, prm.rbuf_in, prm.trace_row);
+  if (blockIdx.x == 0 && prm.record) sample_rows<P, DF>(prm, prm.rbuf_in, prm.trace_row);
 
   // this thread's (element, line) item, the same for every tile
   const int item = threadIdx.x;
@@ -648,8 +943,16 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
           issue_region<P, TE, KAHAN>(txn, tyn, s ? stage0 : stage1, s ? bar0 : bar1, &tm_u, &tm_cu);
       }
     }
-    if (!tile_body<P, TE, NT, KAHAN, NOB == 1>(prm, StepPtrs{prm.stf, prm.rbuf_out, prm.a_out}, tx, ty, s ? stage1 : stage0, bar, parity, ob, bo0, par_o, X1, X2,
-                                               item, el, j, ecx, ecy, wj)) {
+    bool ok;
+    if constexpr (DF)
+      ok = tile_body_df<P, TE, NT, true>(prm, StepPtrs{prm.stf, prm.rbuf_out, prm.a_out}, tx, ty, s ? stage1 : stage0, bar,
+                                         parity, ob, bo0, par_o, reinterpret_cast<float4 *>(X1),
+                                         reinterpret_cast<float4 *>(X2), item, el, j, ecx, ecy);
+    else
+      ok = tile_body<P, TE, NT, KAHAN, NOB == 1>(prm, StepPtrs{prm.stf, prm.rbuf_out, prm.a_out}, tx, ty,
+                                                 s ? stage1 : stage0, bar, parity, ob, bo0, par_o, X1, X2, item, el, j,
+                                                 ecx, ecy, wj);
+    if (!ok) {
       if (threadIdx.x == 0) {
         atomicExch(prm.err, 1);
         // let this CTA's copies in flight land before the shared memory is released
@@ -784,10 +1087,10 @@ __global__ void persist_record_batch(const Params *shots, int nshots, int kblk)
 }
 
 // receiver rows of the last step of a block
-template <int P>
+template <int P, bool DF = false>
 __global__ void persist_record(const Params prm)
 {
-  sample_rows<P>(prm, prm.rbuf_in, prm.trace_row);
+  sample_rows<P, DF>(prm, prm.rbuf_in, prm.trace_row);
 }
 
 }  // namespace se2p

@@ -10,12 +10,17 @@ struct Params {
   int ntx, nty, ntiles;
   // outputs (padded layout, float2 per node)
   float2 *u_out, *w_out, *cu_out, *cw_out;
-  float2 *a_out;                   // optional: a_k (last step of a block)
+  float2 *a_out;                   // optional: a_k (last step of a block); two-float mode: its low
+                                   // parts follow at a_out + ny_g*pitch
   // inputs not loaded by TMA
+  // Two-float mode: every table below is followed in the same allocation by its low
+  // parts (value = hi + lo): minv by ny_g*pitch floats, lam and mu by mx*my, J00 and
+  // iJ00 by mx, J11 and iJ11 by my, src_vals by nsrc*2*npe.
   const float *minv;               // padded, 1/M
   const float *lam, *mu;           // per cell
   const float *J00, *J11, *iJ00, *iJ11;
   float dt, half_dt;
+  float dt_lo, half_dt_lo;         // two-float mode: dt = dt + dt_lo, dt/2 = half_dt + half_dt_lo
   int nsrc;
   const int *src_elem;
   const float *src_vals;           // [nsrc][2*npe]
@@ -24,6 +29,7 @@ struct Params {
   int nrec;
   const int *rec_elem;
   float *rbuf_out;                 // [nrec][npe][6] (u, v, a) of this step's receiver elements
+                                   // (two-float mode: [nrec][npe][12], the 6 high then the 6 low parts)
   const float *rbuf_in;            // previous step's, sampled into trace_row when record != 0
   int record;
   const int *rec_gll;

@@ -9,7 +9,7 @@
  * options it runs the reference demo's physics and prints the same lines and
  * writes the same closestqpsource-receiverCP-uva-*.dat / .mpimeta files.
  *
- * Additions (defaults reproduce the demo): -precision fp64|fp32_kahan|fp32
+ * Additions (defaults reproduce the demo): -precision fp64|fp32_df|fp32_kahan|fp32
  * (fp64 is bit-identical to the reference), -cfl (0.5), -Lx -Ly (2000),
  * -x0 -y0 (-1000), -vp -vs -rho, -cells file (per-cell vp,vs,rho doubles),
  * -problem demo|explosion64|grf2048, -rec_file (x y per line), -block (steps per
@@ -172,7 +172,8 @@ int main(int argc, char **argv)
   opt_int("-bdegree", &p);
   problem = opt_str("-problem", "demo");
   prec_s = opt_str("-precision", "fp64");
-  precision = !strcmp(prec_s, "fp64") ? SE2GPU_FP64 : !strcmp(prec_s, "fp32_kahan") ? SE2GPU_FP32_KAHAN
+  precision = !strcmp(prec_s, "fp64") ? SE2GPU_FP64 : !strcmp(prec_s, "fp32_df") ? SE2GPU_FP32_DF
+            : !strcmp(prec_s, "fp32_kahan") ? SE2GPU_FP32_KAHAN
             : !strcmp(prec_s, "fp32") ? SE2GPU_FP32 : -1;
   if (precision < 0) { fprintf(stderr, "unknown -precision %s\n", prec_s); return 1; }
 

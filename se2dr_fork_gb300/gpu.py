@@ -17,8 +17,8 @@ _LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "lib
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 
-FP64, FP32_KAHAN, FP32 = 64, 33, 32
-PRECISIONS = {"fp64": FP64, "fp32_kahan": FP32_KAHAN, "fp32": FP32}
+FP64, FP32_DF, FP32_KAHAN, FP32 = 64, 34, 33, 32
+PRECISIONS = {"fp64": FP64, "fp32_df": FP32_DF, "fp32_kahan": FP32_KAHAN, "fp32": FP32}
 
 # symbols declared in include/se2gpu.h
 EXPORTS = ["se2gpu_create", "se2gpu_destroy", "se2gpu_last_error", "se2gpu_create_error", "se2gpu_set_stream",
@@ -30,7 +30,7 @@ EXPORTS = ["se2gpu_create", "se2gpu_destroy", "se2gpu_last_error", "se2gpu_creat
            "se2gpu_ensemble_tile_config", "se2gpu_ensemble_advance", "se2gpu_ensemble_enqueue",
            "se2gpu_ensemble_synchronize", "se2gpu_ensemble_get_fields", "se2gpu_ensemble_set_fields",
            "se2gpu_ensemble_info", "se2gpu_norms_device_noalloc",
-           "se2gpu_checkpoint_size", "se2gpu_checkpoint_save", "se2gpu_checkpoint_load"]
+           "se2gpu_checkpoint_size", "se2gpu_checkpoint_save", "se2gpu_checkpoint_load", "se2gpu_pipe_peak"]
 
 
 class _CProblem(C.Structure):
@@ -46,6 +46,19 @@ _lib = None
 
 def lib_path() -> str:
     return _LIB_PATH
+
+
+PIPE_KINDS = {"fp64_mul_add": 0, "fp64_fma": 1, "fp32_mul_add": 2, "fp32_fma": 3}
+
+
+def pipe_peak(kind: str) -> float:
+    """Measured arithmetic operations per second of one pipe mix on the current device
+    (se2gpu_pipe_peak; a fused multiply-add counts two)."""
+    out = C.c_double(0.0)
+    rc = lib().se2gpu_pipe_peak(PIPE_KINDS[kind], C.byref(out))
+    if rc != 0:
+        raise GpuError(f"se2gpu_pipe_peak failed ({rc}): {lib().se2gpu_last_error(None).decode()}")
+    return out.value
 
 
 def lib():
@@ -92,6 +105,7 @@ def lib():
         L.se2gpu_ensemble_set_fields.argtypes = [vp, C.c_int, _dp, _dp, _dp]
         L.se2gpu_ensemble_info.argtypes = [vp, C.POINTER(C.c_long)]
         L.se2gpu_norms_device_noalloc.argtypes = [vp, vp, C.c_long, vp, _dp]
+        L.se2gpu_pipe_peak.argtypes = [C.c_int, _dp]
         L.se2gpu_checkpoint_size.argtypes = [vp]
         L.se2gpu_checkpoint_size.restype = C.c_long
         L.se2gpu_checkpoint_save.argtypes = [vp, vp, C.c_long]

@@ -113,7 +113,7 @@ def test_create_validates_the_problem_without_gpu(gpu_lib, case):
         pr.mass = None
         msg = b"missing problem table"
     h = ctypes.c_void_p()
-    for precision in (64, 33, 32):
+    for precision in (64, 34, 33, 32):
         rc = gpu.lib().se2gpu_create(ctypes.byref(pr), precision, cap, ctypes.byref(h))
         assert rc == -1 and not h.value, case
         assert msg in gpu.lib().se2gpu_create_error(), gpu.lib().se2gpu_create_error()

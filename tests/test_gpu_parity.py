@@ -339,7 +339,7 @@ def test_tile_config_info(p):
     assert f64["owned_buffers"] == 0 and f64["ctas_per_sm"] == 0
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32_kahan", "fp32"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32_df", "fp32_kahan", "fp32"])
 def test_checkpoint_resume_is_bitwise(precision):
     """Stop after 37 steps, checkpoint, resume in a new handle: identical traces and fields."""
     d = load("hetero_p4")
@@ -396,3 +396,24 @@ def test_alternative_source_representations_run(impl):
     t32 = G.Solver(H.Setup(sp), "fp32_kahan").run()
     ok, errs = fp32_errors_ok(t32, t1, k=2 * np.pi * 8.0 / sp.vs)
     assert ok, errs
+
+
+@pytest.mark.parametrize("precision", [64, 34, 33, 32])
+def test_create_rejects_a_non_positive_mass_on_the_gpu(precision):
+    """Where the device reads pageable host memory the FP32 modes check the mass in the
+    kernel that forms 1/M (no host pass); the first bad node is reported either way, and
+    a later create on good input succeeds."""
+    import ctypes
+    su = H.Setup(S.demo(4, 3, p=2, tmax=1.0).replace(nt=4))
+    pr, keep = G._problem(su)
+    m = np.array(su.mass)
+    m[7] = 0.0
+    m[9] = -1.0
+    m[11] = np.nan
+    pr.mass = m.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    h = ctypes.c_void_p()
+    rc = G.lib().se2gpu_create(ctypes.byref(pr), precision, 4, ctypes.byref(h))
+    assert rc == -1 and not h.value
+    assert b"node 7 is not positive" in G.lib().se2gpu_create_error(), G.lib().se2gpu_create_error()
+    name = {64: "fp64", 34: "fp32_df", 33: "fp32_kahan", 32: "fp32"}[precision]
+    assert G.Solver(su, name).run().shape[0] == su.nsteps
