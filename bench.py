@@ -56,7 +56,42 @@ def alg_bytes_per_node(precision: str, ne: int, nnodes: int) -> float:
         return 2 * 3 * 16 + 8 + 16 * cell          # u,v,a (double2) in+out, M, (lambda, mu)
     if precision == "fp32_kahan":
         return 2 * 4 * 8 + 4 + 8 * cell            # leapfrog u,w,cu,cw (float2) in+out, 1/M, (lambda, mu)
+    if precision == "fp32_df":
+        return 2 * 4 * 8 + 8 + 16 * cell           # the same state, 1/M and (lambda, mu) with their low parts
     return 2 * 2 * 8 + 4 + 8 * cell                # leapfrog u,w (float2) in+out, 1/M, (lambda, mu)
+
+
+def fp64_ops_per_node(p: int) -> float:
+    """Algorithmic FP64 operations per node and step of the reference's arithmetic
+    (se2wave.c:1321-1417 and 4724-4745) with its dense element sums restricted to the
+    terms that are not exact zeros (the row and column of each point), as the FP64 kernel
+    evaluates them, and without any halo recompute.  Per GLL point: strains 2 x N1 + 2 x N1
+    + 4 x N1 (the shear sum over row and column with the diagonal term) multiplies and
+    adds, c11 and the three stresses 9 -> 8 N1 + 9.  Per element node: the weak divergence
+    over the 2 N1 - 1 points of its row and column, x and y: 6 per off-diagonal point and
+    10 at the node itself -> 12 N1 - 2.  Per node: the element sums (N1^2 / p^2
+    contributions per component), the three AXPYs of the predictor (12), f + g (4), a = f / M
+    (2 divisions) and the corrector (4)."""
+    n1 = p + 1
+    per_element = n1 * n1 * (8 * n1 + 9) + n1 * n1 * (12 * n1 - 2)
+    return per_element / (p * p) + 2.0 * n1 * n1 / (p * p) + 12 + 4 + 2 + 4
+
+
+def df_ops_per_node(p: int) -> float:
+    """Algorithmic FP32 arithmetic instructions per node and step of the two-float mode (no
+    halo recompute): per (element, line) item, the displacement differences (TwoSum + 2,
+    x and y: 16 p per direction), the derivative contractions as compensated dot products
+    (12 per term, N1 p terms per component and direction) with one TwoSum normalisation per
+    output (6), the Hooke stress and factors (145 per point, 29 per item), the xi and eta
+    divergences (24 N1^2 + 12 N1 each); per node the element sum (11 per extra
+    contribution and component), a = f / M (14) and the two updates (36 each)."""
+    n1 = p + 1
+    grad = 2 * (16 * p + 24 * p * n1 + 12 * n1)
+    stress = 145 * n1 + 29
+    div = 2 * (24 * n1 * n1 + 12 * n1)
+    per_element = n1 * (grad + stress + div)
+    extra = 2.0 * (n1 * n1 / (p * p) - 1.0) * 11
+    return per_element / (p * p) + extra + 14 + 36 + 36
 
 
 def reference_bytes_per_node(precision: str, ne: int, nnodes: int) -> float:
@@ -245,8 +280,17 @@ def run_ours(args, rank, world):
     tuned = None
     if args.autotune and args.precision != "fp64":
         tuned = autotune.tune(setup, args.precision, steps=10)
-    for prec in [args.precision] + (["fp64"] if args.precision != "fp64" and not args.no_fp64 else []):
-        k = args.steps if prec == args.precision else max(3, args.steps // 8)
+    legs = [args.precision] + (["fp64"] if args.precision != "fp64" and not args.no_fp64 else [])
+    if args.precision != "fp32_df" and not args.no_df:
+        legs.append("fp32_df")
+    pipe = {}
+    for kind in ("fp64_mul_add", "fp32_mul_add"):
+        try:
+            pipe[kind] = G.pipe_peak(kind)
+        except Exception:
+            pipe[kind] = None
+    for prec in legs:
+        k = args.steps if prec == args.precision else max(3, args.steps // (8 if prec == "fp64" else 2))
         sol = G.Solver(setup, prec, trace_capacity=k + args.warmup + 2)
         if prec != "fp64":
             if args.tile_config >= 0:
@@ -274,6 +318,17 @@ def run_ours(args, rank, world):
                                       "traffic_note": "ncu DRAM bytes per node at 1024^2 x nodes (bytes per launch)",
                                       "alg_bytes_per_node": b, "peak_kind": peak_kind,
                                       "reference_formulation": reference_formulation(prec, ne, nnodes, per, hbm)}}
+        # the arithmetic roof of the kernels that HBM does not bound, against the pipe rate
+        # measured on this device (se2gpu_pipe_peak)
+        ops, kind = {"fp64": (fp64_ops_per_node, "fp64_mul_add"), "fp32_df": (df_ops_per_node, "fp32_mul_add")}.get(
+            prec, (None, None))
+        if ops and pipe.get(kind):
+            ach = ops(args.degree) * nnodes / per / 1e12
+            results[prec]["pipe_roofline"] = {
+                "bound": "fp64 pipe" if prec == "fp64" else "fp32 pipe", "achieved": ach, "peak": pipe[kind] / 1e12,
+                "unit": "Tops/s", "frac": ach / (pipe[kind] / 1e12), "ops_per_node": ops(args.degree),
+                "peak_kind": "measured (se2gpu_pipe_peak %s)" % kind,
+                "note": "algorithmic arithmetic operations per node (no halo recompute) x nodes / step time"}
 
     # end to end through the C-ABI: create (upload from host) + K steps + traces read back + destroy
     prec = args.precision
@@ -290,9 +345,11 @@ def run_ours(args, rank, world):
     sol.close()
     torch.cuda.synchronize()
     e2e_s = tmax(time.perf_counter() - t0)
-    tsize = 8 if prec == "fp64" else 4
-    h2d = (nnodes * tsize + 2 * ne * tsize + 4 * (setup.mx + setup.my) * tsize + 2 * setup.npe * (tsize + 8)
-           + setup.nsrc * 2 * setup.npe * tsize + 12 * setup.nrec + 8 * setup.nsrc * args.steps)
+    # bytes of the caller's FP64 host arrays that se2gpu_create and advance read: the mass, the
+    # cell Lame parameters, the Jacobians, D and the weights, the source values, the receiver
+    # indices and the STF values of every step (the FP32 modes convert on the device)
+    h2d = (nnodes * 8 + 2 * ne * 8 + 4 * (setup.mx + setup.my) * 8 + 2 * setup.npe * 16
+           + setup.nsrc * 2 * setup.npe * 8 + 12 * setup.nrec + 8 * setup.nsrc * args.steps)
     d2h = tr.shape[0] * 7 * setup.nrec * 8
 
     if rank != 0:
@@ -319,7 +376,7 @@ def run_ours(args, rank, world):
                                    f"Gaussian-random-field Vp (mean 5000, 10% std, corr 8 cells), Vp/Vs 1.73, "
                                    f"rho 2700, explosive Ricker f0 8 Hz, 64 receivers",
                        "precision": prec, "nodes": nnodes, "dof": dof, "parallelism": f"replicas x{world}",
-                       "l2": "inputs larger than L2 (state %.1f GB)" % ({"fp32_kahan": 8, "fp32": 4, "fp64": 6}[prec]
+                       "l2": "inputs larger than L2 (state %.1f GB)" % ({"fp32_kahan": 8, "fp32_df": 8, "fp32": 4, "fp64": 6}[prec]
                                                                        * nnodes * (4 if prec != 'fp64' else 8) * 2 / 1e9)},
             "roofline": head["roofline"], "clocks": head["clocks"], "gpu_launches": head["launches"],
             "tile": head.get("tile"), "autotune": tuned,
@@ -327,10 +384,13 @@ def run_ours(args, rank, world):
                     "d2h_bytes_per_step": d2h / args.steps, "seconds": e2e_s,
                     "includes": "se2gpu_create (upload of the set-up from host memory), advance, traces, destroy"},
             "cpu_baseline": cpu}
-    if "fp64" in results and args.precision != "fp64":
-        r = results["fp64"]
-        line["fp64"] = {"value": r["value"], "ms_per_step": r["ms_per_step"], "steps": r["steps"],
-                        "roofline": r["roofline"], "clocks": r["clocks"]}
+    for leg in ("fp64", "fp32_df"):
+        if leg in results and args.precision != leg:
+            r = results[leg]
+            line[leg] = {"value": r["value"], "ms_per_step": r["ms_per_step"], "steps": r["steps"],
+                         "roofline": r["roofline"], "pipe_roofline": r.get("pipe_roofline"), "clocks": r["clocks"]}
+    if "pipe_roofline" in head:
+        line["pipe_roofline"] = head["pipe_roofline"]
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -669,10 +729,11 @@ def main():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--precision", choices=["fp32_kahan", "fp32", "fp64"], default="fp32_kahan")
+    ap.add_argument("--precision", choices=["fp32_kahan", "fp32", "fp32_df", "fp64"], default="fp32_kahan")
     ap.add_argument("--mx", type=int, default=2048, help="elements per side (default: the 2048^2 workload)")
     ap.add_argument("--degree", type=int, default=4, help="polynomial degree of the single-solve run (default 4)")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-df", action="store_true", help="skip the two-float FP32 leg")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-rows", type=int, default=32)
     ap.add_argument("--cpu-steps", type=int, default=6)
