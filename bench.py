@@ -100,9 +100,10 @@ def reference_bytes_per_node(precision: str, ne: int, nnodes: int) -> float:
     and v), 1/M and the cell's (lambda, mu).  The kick-drift state above needs no a, so it moves
     fewer bytes for the same DOF-updates; this count is the one to compare other
     implementations of the reference's scheme against."""
-    words = {"fp64": 13, "fp32": 13, "fp32_kahan": 21}[precision]
+    words = {"fp64": 13, "fp32": 13, "fp32_kahan": 21, "fp32_df": 22}[precision]   # two-float: 1/M's low part
+    cell_words = 4 if precision == "fp32_df" else 2
     wb = 8 if precision == "fp64" else 4
-    return (words + 2 * ne / nnodes) * wb
+    return (words + cell_words * ne / nnodes) * wb
 
 
 def reference_formulation(precision: str, ne: int, nnodes: int, per_step: float, hbm: float) -> dict:

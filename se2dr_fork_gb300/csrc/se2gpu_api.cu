@@ -155,18 +155,32 @@ static void host_parallel(long n, F fn, long minchunk = 1L << 20)
 // division and the conversion to float round as on the host, so the values are the same.
 // minv_lo (two-float mode, else null): the remainder 1/M - minv, rounded to float.  *bad
 // receives the smallest node whose mass is not positive and finite (it starts at ~0).
-__global__ void k_minv_from_host(const double *__restrict__ mass, long nx_g, long ny_g, int pitch,
-                                 float *__restrict__ minv, float *__restrict__ minv_lo, unsigned long long *bad)
+// Block (bx, by) takes 1024 padded columns of rows by, by + gridDim.y, ..., four per thread,
+// the four host loads issued before any is used so that more of the host link's latency is
+// in flight.
+__global__ void __launch_bounds__(256) k_minv_from_host(const double *__restrict__ mass, long nx_g, long ny_g,
+                                                        int pitch, float *__restrict__ minv,
+                                                        float *__restrict__ minv_lo, unsigned long long *bad)
 {
-  const long np = ny_g * (long)pitch;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < np; i += (long)gridDim.x * blockDim.x) {
-    const long y = i / pitch, x = i - y * pitch;
-    const double m = (x < nx_g) ? mass[y * nx_g + x] : 1.0;
-    if (!(m > 0.0) || !isfinite(m)) atomicMin(bad, (unsigned long long)(y * nx_g + x));
-    const double r = (x < nx_g) ? 1.0 / m : 0.0;
+  for (long y = blockIdx.y; y < ny_g; y += gridDim.y) {
+  const double *row = mass + y * nx_g;
+  double m[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const long x = (long)blockIdx.x * 1024 + k * 256 + threadIdx.x;
+    m[k] = (x < nx_g) ? row[x] : 1.0;
+  }
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const long x = (long)blockIdx.x * 1024 + k * 256 + threadIdx.x;
+    if (x >= pitch) continue;
+    const long i = y * pitch + x;
+    if (!(m[k] > 0.0) || !isfinite(m[k])) atomicMin(bad, (unsigned long long)(y * nx_g + x));
+    const double r = (x < nx_g) ? 1.0 / m[k] : 0.0;
     const float h = __double2float_rn(r);
     minv[i] = h;
     if (minv_lo) minv_lo[i] = __double2float_rn(__dsub_rn(r, (double)h));
+  }
   }
 }
 
@@ -554,12 +568,42 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
     h->pitch = (int)((nx_g + 1 + 15) / 16 * 16);   // >= 1 padding node: paired reads stay in the row
     const size_t np = (size_t)ny_g * h->pitch;
     for (int b = 0; b < 2; b++) {
-      TRY(dzero(h, (void **)&h->pu[b], np * 8));
-      TRY(dzero(h, (void **)&h->pw[b], np * 8));
-      if (kahan) { TRY(dzero(h, (void **)&h->pcu[b], np * 8)); TRY(dzero(h, (void **)&h->pcw[b], np * 8)); }
+      TRY(dalloc(h, (void **)&h->pu[b], np * 8));
+      TRY(dalloc(h, (void **)&h->pw[b], np * 8));
+      if (kahan) { TRY(dalloc(h, (void **)&h->pcu[b], np * 8)); TRY(dalloc(h, (void **)&h->pcw[b], np * 8)); }
       TRY(dzero(h, (void **)&h->rbuf[b], (size_t)P->nrec * npe * rbuf_values(h) * 4));
     }
-    TRY(dzero(h, (void **)&h->pa, np * 8 * (df ? 2 : 1)));   // two-float mode: low parts after the high
+    TRY(dalloc(h, (void **)&h->pa, np * 8 * (df ? 2 : 1)));   // two-float mode: low parts after the high
+    // The fields start at zero: the first buffer set and a are cleared.  The second set is
+    // written at every mesh node by the first step before anything reads it (the tile copies
+    // never read past the mesh), so only its row padding is cleared, to keep checkpoints
+    // deterministic.  The clearing runs on a second stream, beside the kernels below that
+    // read the caller's arrays over the host link, and the handle's stream waits for it.
+    {
+      cudaStream_t side = nullptr;
+      cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+      cudaError_t e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev0, cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev1, cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventRecord(ev0, h->stream);   // the allocations above
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(side, ev0, 0);
+      float2 *full[5] = {h->pu[0], h->pw[0], kahan ? h->pcu[0] : nullptr, kahan ? h->pcw[0] : nullptr, h->pa};
+      for (int f = 0; f < 5 && e == cudaSuccess; f++)
+        if (full[f]) e = cudaMemsetAsync(full[f], 0, np * 8 * ((f == 4 && df) ? 2 : 1), side);
+      float2 *pad[4] = {h->pu[1], h->pw[1], kahan ? h->pcu[1] : nullptr, kahan ? h->pcw[1] : nullptr};
+      for (int f = 0; f < 4 && e == cudaSuccess; f++)
+        if (pad[f]) e = cudaMemset2DAsync(pad[f] + nx_g, (size_t)h->pitch * 8, 0, (size_t)(h->pitch - nx_g) * 8, ny_g, side);
+      if (e == cudaSuccess) e = cudaEventRecord(ev1, side);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, ev1, 0);
+      if (ev0) cudaEventDestroy(ev0);
+      if (ev1) cudaEventDestroy(ev1);
+      if (side) cudaStreamDestroy(side);   // released once its work is done
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        fail(h, SE2GPU_ERR_CUDA, "clearing the state: %s", cudaGetErrorString(e));
+        TRY(SE2GPU_ERR_CUDA);
+      }
+    }
     if (h->pageable) {
       // the device reads the mass where it lies (no staging copy of the whole array)
       TRY(dalloc(h, (void **)&h->pminv, np * 4 * (df ? 2 : 1)));
@@ -568,8 +612,8 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
         fail(h, SE2GPU_ERR_CUDA, "mass check set-up");
         TRY(SE2GPU_ERR_CUDA);
       }
-      k_minv_from_host<<<4 * h->nsm, 256, 0, h->stream>>>(P->mass, nx_g, ny_g, h->pitch, h->pminv,
-                                                          df ? h->pminv + np : nullptr, h->mass_bad);
+      k_minv_from_host<<<dim3((h->pitch + 1023) / 1024, (unsigned)std::min(ny_g, 65535L)), 256, 0, h->stream>>>(
+          P->mass, nx_g, ny_g, h->pitch, h->pminv, df ? h->pminv + np : nullptr, h->mass_bad);
       if (cudaGetLastError() != cudaSuccess) {
         fail(h, SE2GPU_ERR_CUDA, "1/M from host memory");
         TRY(SE2GPU_ERR_CUDA);

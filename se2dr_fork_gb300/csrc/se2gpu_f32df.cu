@@ -38,18 +38,18 @@ struct DfEntry {
 
 // registers sized for 2 CTAs per SM at most (1 with 384 threads or more): the pairs
 // double most live values
-template <int P, int TE, int NT>
+template <int P, int TE, int NT, bool WE>
 DfEntry df_entry()
 {
   typedef Layout<P, TE, true, 1, true> L;
   constexpr int MS = min_blocks(L::TOTAL);
   constexpr int M = (NT >= 384) ? 1 : (MS < 2 ? MS : 2);
-  return DfEntry{P, TE, NT, L::TOTAL, (const void *)persist_step<P, TE, NT, true, 1, M, true>};
+  return DfEntry{P, TE, NT, L::TOTAL, (const void *)persist_step<P, TE, NT, true, 1, M, true, WE>};
 }
 
 const DfEntry *df_table(int *n)
 {
-#define SE2P_DF_ENTRY(P, TE, NT, NOB, MINB) df_entry<P, TE, NT>(),
+#define SE2P_DF_ENTRY(P, TE, NT, NOB, MINB, WE) df_entry<P, TE, NT, (WE) != 0>(),
   static DfEntry t[] = {SE2P_CONFIGS(SE2P_DF_ENTRY)};
 #undef SE2P_DF_ENTRY
   *n = (int)(sizeof(t) / sizeof(t[0]));

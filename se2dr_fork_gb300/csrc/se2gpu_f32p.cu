@@ -30,7 +30,7 @@ struct Entry {
   const void *bfn[2];             // persist_batch<...> [kahan]
 };
 
-template <int P, int TE, int NT, int NOB = owned_buffers(P), int MINB = 0>
+template <int P, int TE, int NT, int NOB = owned_buffers(P), int MINB = 0, bool WE = false>
 static Entry entry()
 {
   constexpr int M0 = MINB ? MINB : min_blocks(Layout<P, TE, false, NOB>::TOTAL);
@@ -43,16 +43,16 @@ static Entry entry()
   e.smem[1] = Layout<P, TE, true, NOB>::TOTAL;
   e.bsmem[0] = Layout<P, TE, false, NOB>::BATCH_TOTAL;
   e.bsmem[1] = Layout<P, TE, true, NOB>::BATCH_TOTAL;
-  e.fn[0] = (const void *)persist_step<P, TE, NT, false, NOB, M0>;
-  e.fn[1] = (const void *)persist_step<P, TE, NT, true, NOB, M1>;
-  e.bfn[0] = (const void *)persist_batch<P, TE, NT, false, NOB, B0>;
-  e.bfn[1] = (const void *)persist_batch<P, TE, NT, true, NOB, B1>;
+  e.fn[0] = (const void *)persist_step<P, TE, NT, false, NOB, M0, false, WE>;
+  e.fn[1] = (const void *)persist_step<P, TE, NT, true, NOB, M1, false, WE>;
+  e.bfn[0] = (const void *)persist_batch<P, TE, NT, false, NOB, B0, WE>;
+  e.bfn[1] = (const void *)persist_batch<P, TE, NT, true, NOB, B1, WE>;
   return e;
 }
 
 static const Entry *table(int *n)
 {
-#define SE2P_ENTRY(P, TE, NT, NOB, MINB) entry<P, TE, NT, (NOB) ? (NOB) : owned_buffers(P), MINB>(),
+#define SE2P_ENTRY(P, TE, NT, NOB, MINB, WE) entry<P, TE, NT, (NOB) ? (NOB) : owned_buffers(P), MINB, (WE) != 0>(),
   static Entry t[] = {SE2P_CONFIGS(SE2P_ENTRY)};
 #undef SE2P_ENTRY
   *n = (int)(sizeof(t) / sizeof(t[0]));

@@ -117,6 +117,10 @@ struct Geo {
   static constexpr int XS = NPE + (P == 1 ? 2 : P == 3 ? 3 : P == 6 ? 6 : P == 7 ? 7 : P == 8 ? 8 : 0);
   static constexpr int NEX = TE + 1, NE = NEX * NEX;      // elements incl. halo
   static constexpr int ITEMS = NE * N1;                   // (element, line) work items
+  // warp-aligned mapping: EPW whole elements per warp (their N1 lines in consecutive
+  // lanes), NW warps; the element phases then exchange values within a warp only
+  static constexpr int EPW = 32 / N1;
+  static constexpr int NW = (NE + EPW - 1) / EPW;
   // region box (u, cu): the x start is rounded down to an even node so the copy
   // starts on a 16-byte boundary; one extra column absorbs the shift and two
   // more keep the node phase's paired (16-byte) reads inside the box
@@ -270,10 +274,12 @@ struct StepPtrs {
 
 // one tile: prefetch of global values, wait for the tile's copies, the three
 // element phases and the node phase.  Returns false when the bounded wait expired.
-template <int P, int TE, int NT, bool KAHAN, bool OWAIT>
+// WE: the warp-aligned item mapping (every element's lines in one warp), whose element
+// phases synchronise within the warp instead of the block
+template <int P, int TE, int NT, bool KAHAN, bool OWAIT, bool WE = false>
 __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp, int tx, int ty, const unsigned char *st, uint32_t bar,
                                           uint32_t parity, const unsigned char *ob, uint32_t bar_o, uint32_t par_o,
-                                          float2 *X1, float2 *X2, int item, int el, int j, int ecx, int ecy, float wj)
+                                          float2 *X1, float2 *X2, bool valid, int el, int j, int ecx, int ecy, float wj)
 {
   typedef Geo<P, TE> G;
   typedef Layout<P, TE, KAHAN> L;
@@ -283,7 +289,7 @@ __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp,
   const TileBox b = tile_box<P, TE>(prm, tx, ty);
   const int t = ty * prm.ntx + tx;
   const int xoff = b.EX0 * P - b.RXa;   // region-box column of the first region node
-  const bool active = (item < G::ITEMS) && (ecx < b.NEXa) && (ecy < b.NEYa);
+  const bool active = valid && (ecx < b.NEXa) && (ecy < b.NEYa);
   const int ex = b.EX0 + ecx, ey = b.EY0 + ecy;
   // global loads issued before the wait: per-element constants, the tile's
   // source/receiver list bounds and 1/M of this thread's owned node pairs
@@ -376,7 +382,7 @@ __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp,
       }
     }
   }
-  __syncthreads();
+  if constexpr (WE) __syncwarp(); else __syncthreads();
 
   // ---- 2. stress at the row's points; xi divergence; eta fluxes to X2 ---
   if (active) {
@@ -402,7 +408,7 @@ __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp,
       X1[el * XS + a + j * N1] = make_float2(rx, ry);
     }
   }
-  __syncthreads();
+  if constexpr (WE) __syncwarp(); else __syncthreads();
 
   // ---- 3. eta part of the divergence along column j (its 5 fluxes), added to X1 -----
   if (active) {
@@ -646,10 +652,10 @@ __device__ __forceinline__ tf tf_from_double(double v)
 // float4 = (x.h, y.h, x.l, y.l)) and the tables' low parts read beside their high
 // parts.  The state keeps the Kahan mode's storage (value = hi - c), so fields,
 // norms and checkpoints are shared with that mode.
-template <int P, int TE, int NT, bool OWAIT>
+template <int P, int TE, int NT, bool OWAIT, bool WE = false>
 __device__ __forceinline__ bool tile_body_df(const Params &prm, const StepPtrs stp, int tx, int ty, const unsigned char *st,
                                              uint32_t bar, uint32_t parity, const unsigned char *ob, uint32_t bar_o,
-                                             uint32_t par_o, float4 *X1, float4 *X2, int item, int el, int j, int ecx,
+                                             uint32_t par_o, float4 *X1, float4 *X2, bool valid, int el, int j, int ecx,
                                              int ecy)
 {
   typedef Geo<P, TE> G;
@@ -659,7 +665,7 @@ __device__ __forceinline__ bool tile_body_df(const Params &prm, const StepPtrs s
   const TileBox b = tile_box<P, TE>(prm, tx, ty);
   const int t = ty * prm.ntx + tx;
   const int xoff = b.EX0 * P - b.RXa;
-  const bool active = (item < G::ITEMS) && (ecx < b.NEXa) && (ecy < b.NEYa);
+  const bool active = valid && (ecx < b.NEXa) && (ecy < b.NEYa);
   const int ex = b.EX0 + ecx, ey = b.EY0 + ecy;
   const size_t ncell = (size_t)prm.mx * prm.my;
   tf lam{0.f, 0.f}, mu{0.f, 0.f}, ix{0.f, 0.f}, iy{0.f, 0.f}, detJ{0.f, 0.f};
@@ -732,7 +738,7 @@ __device__ __forceinline__ bool tile_body_df(const Params &prm, const StepPtrs s
       }
     }
   }
-  __syncthreads();
+  if constexpr (WE) __syncwarp(); else __syncthreads();
 
   // ---- 2. stress at the row's points; xi divergence; eta fluxes to X2 ---
   if (active) {
@@ -769,7 +775,7 @@ __device__ __forceinline__ bool tile_body_df(const Params &prm, const StepPtrs s
       X1[el * XS + a + j * N1] = make_float4(rx.h, ry.h, rx.l, ry.l);
     }
   }
-  __syncthreads();
+  if constexpr (WE) __syncwarp(); else __syncthreads();
 
   // ---- 3. eta part of the divergence along column j, added to X1 -----
   if (active) {
@@ -870,9 +876,27 @@ __device__ __forceinline__ bool tile_body_df(const Params &prm, const StepPtrs s
   return true;
 }
 
-// DF: the two-float mode (KAHAN storage, tile_body_df)
+// this thread's (element, line) work item, the same for every tile
+template <int P, int TE, bool WE>
+__device__ __forceinline__ void item_of(int &el, int &j, bool &valid)
+{
+  typedef Geo<P, TE> G;
+  constexpr int N1 = G::N1;
+  if constexpr (WE) {
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, sub = lane / N1;
+    el = w * G::EPW + sub;
+    j = lane - sub * N1;
+    valid = (sub < G::EPW) && (el < G::NE);
+  } else {
+    el = threadIdx.x / N1;
+    j = threadIdx.x - el * N1;
+    valid = threadIdx.x < G::ITEMS;
+  }
+}
+
+// DF: the two-float mode (KAHAN storage, tile_body_df); WE: the warp-aligned item mapping
 template <int P, int TE, int NT, bool KAHAN, int NOB = owned_buffers(P),
-          int MINB = min_blocks(Layout<P, TE, KAHAN, NOB>::TOTAL), bool DF = false>
+          int MINB = min_blocks(Layout<P, TE, KAHAN, NOB>::TOTAL), bool DF = false, bool WE = false>
 __global__ void __launch_bounds__(NT, MINB)
 persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ CUtensorMap tm_cu,
              const __grid_constant__ CUtensorMap tm_w, const __grid_constant__ CUtensorMap tm_cw,
@@ -881,7 +905,7 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
   typedef Geo<P, TE> G;
   typedef Layout<P, TE, KAHAN, NOB, DF> L;
   constexpr int N1 = G::N1, NEX = G::NEX;
-  static_assert(NT >= G::ITEMS, "one (element, line) item per thread");
+  static_assert(WE ? NT >= 32 * G::NW : NT >= G::ITEMS, "one (element, line) item per thread");
   static_assert(NOB == 1 || NOB == 2, "one or two owned-box buffers");
   static_assert(!DF || (KAHAN && NOB == 1), "the two-float mode keeps the Kahan storage and one owned buffer");
   const float *W = c_w[P - 1];
@@ -906,11 +930,11 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
   __syncthreads();
   if (blockIdx.x == 0 && prm.record) sample_rows<P, DF>(prm, prm.rbuf_in, prm.trace_row);
 
-  // this thread's (element, line) item, the same for every tile
-  const int item = threadIdx.x;
-  const int el = item / N1, j = item - (item / N1) * N1;
+  int el, j;
+  bool valid;
+  item_of<P, TE, WE>(el, j, valid);
   const int ecy = el / NEX, ecx = el - (el / NEX) * NEX;
-  const float wj = (item < G::ITEMS) ? W[j] : 0.f;
+  const float wj = valid ? W[j] : 0.f;
 
   // tile coordinates advance by the grid size without a division per tile
   int t = blockIdx.x;
@@ -945,13 +969,13 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
     }
     bool ok;
     if constexpr (DF)
-      ok = tile_body_df<P, TE, NT, true>(prm, StepPtrs{prm.stf, prm.rbuf_out, prm.a_out}, tx, ty, s ? stage1 : stage0, bar,
-                                         parity, ob, bo0, par_o, reinterpret_cast<float4 *>(X1),
-                                         reinterpret_cast<float4 *>(X2), item, el, j, ecx, ecy);
+      ok = tile_body_df<P, TE, NT, true, WE>(prm, StepPtrs{prm.stf, prm.rbuf_out, prm.a_out}, tx, ty, s ? stage1 : stage0,
+                                             bar, parity, ob, bo0, par_o, reinterpret_cast<float4 *>(X1),
+                                             reinterpret_cast<float4 *>(X2), valid, el, j, ecx, ecy);
     else
-      ok = tile_body<P, TE, NT, KAHAN, NOB == 1>(prm, StepPtrs{prm.stf, prm.rbuf_out, prm.a_out}, tx, ty,
-                                                 s ? stage1 : stage0, bar, parity, ob, bo0, par_o, X1, X2, item, el, j,
-                                                 ecx, ecy, wj);
+      ok = tile_body<P, TE, NT, KAHAN, NOB == 1, WE>(prm, StepPtrs{prm.stf, prm.rbuf_out, prm.a_out}, tx, ty,
+                                                     s ? stage1 : stage0, bar, parity, ob, bo0, par_o, X1, X2, valid, el,
+                                                     j, ecx, ecy, wj);
     if (!ok) {
       if (threadIdx.x == 0) {
         atomicExch(prm.err, 1);
@@ -981,14 +1005,14 @@ __device__ __forceinline__ const float *batch_rbuf(const Params &sh, int kblk)
 }
 
 template <int P, int TE, int NT, bool KAHAN, int NOB = owned_buffers(P),
-          int MINB = min_blocks(Layout<P, TE, KAHAN, NOB>::TOTAL)>
+          int MINB = min_blocks(Layout<P, TE, KAHAN, NOB>::TOTAL), bool WE = false>
 __global__ void __launch_bounds__(NT, MINB)
 persist_batch(const __grid_constant__ BatchArgs ba)
 {
   typedef Geo<P, TE> G;
   typedef Layout<P, TE, KAHAN, NOB> L;
   constexpr int N1 = G::N1, NEX = G::NEX;
-  static_assert(NT >= G::ITEMS, "one (element, line) item per thread");
+  static_assert(WE ? NT >= 32 * G::NW : NT >= G::ITEMS, "one (element, line) item per thread");
   static_assert(NOB == 1 || NOB == 2, "one or two owned-box buffers");
   const float *W = c_w[P - 1];
   extern __shared__ __align__(128) unsigned char smem[];
@@ -1015,10 +1039,11 @@ persist_batch(const __grid_constant__ BatchArgs ba)
       if (q.nrec > 0) sample_rows<P>(q, batch_rbuf(q, ba.kblk - 1), q.trace_row + (size_t)(ba.kblk - 1) * 7 * q.nrec);
     }
 
-  const int item = threadIdx.x;
-  const int el = item / N1, j = item - (item / N1) * N1;
+  int el, j;
+  bool valid;
+  item_of<P, TE, WE>(el, j, valid);
   const int ecy = el / NEX, ecx = el - (el / NEX) * NEX;
-  const float wj = (item < G::ITEMS) ? W[j] : 0.f;
+  const float wj = valid ? W[j] : 0.f;
 
   // The shots' parameters are a kernel parameter (constant bank), so a tile reads
   // its shot's directly.  Every thread keeps the work items of this tile and the
@@ -1062,8 +1087,8 @@ persist_batch(const __grid_constant__ BatchArgs ba)
     const Params &sp = ba.shots[cur.x];
     const StepPtrs stp{sp.stf + (size_t)ba.kblk * sp.nsrc, const_cast<float *>(batch_rbuf(sp, ba.kblk)),
                        ba.write_a ? sp.a_out : nullptr};
-    if (!tile_body<P, TE, NT, KAHAN, NOB == 1>(sp, stp, cur.y & 0xFFFF, cur.y >> 16, s ? stage1 : stage0, bar, parity,
-                                               ob, bo0, par_o, X1, X2, item, el, j, ecx, ecy, wj)) {
+    if (!tile_body<P, TE, NT, KAHAN, NOB == 1, WE>(sp, stp, cur.y & 0xFFFF, cur.y >> 16, s ? stage1 : stage0, bar,
+                                                   parity, ob, bo0, par_o, X1, X2, valid, el, j, ecx, ecy, wj)) {
       if (threadIdx.x == 0) {
         atomicExch(ba.err, 1);
         mbar_wait_bounded(bar, parity);

@@ -9,20 +9,24 @@ namespace se2p {
 
 // Tile configurations of the persistent kernels, X(degree, elements per tile edge,
 // threads, owned-box buffers (0: owned_buffers(degree)), CTAs per SM the registers are
-// sized for (0: as many as the shared memory allows, up to 3)).  Every (element, line)
-// item of a tile gets its own thread: threads >= (edge + 1)^2 (degree + 1).  Degree 4:
-// 7x7 with one owned buffer kept at 2 CTAs per SM (92 registers) is the fastest; sized
-// for 3 CTAs it is capped at 64 registers and runs slower.  The two-float mode uses the
-// same list with one owned buffer.
-#define SE2P_CONFIGS(X)                                                                   \
-  X(1, 15, 512, 0, 0) X(1, 11, 288, 0, 0)                                                 \
-  X(2, 12, 512, 2, 2) X(2, 10, 384, 0, 0) X(2, 8, 256, 0, 0)                              \
-  X(3, 7, 256, 0, 0) X(3, 8, 352, 0, 0)                                                   \
-  X(4, 7, 320, 1, 2) X(4, 7, 320, 2, 0) X(4, 6, 256, 2, 0) X(4, 8, 416, 0, 0)             \
-  X(5, 6, 320, 0, 0) X(5, 5, 224, 0, 0)                                                   \
-  X(6, 5, 256, 0, 0) X(6, 4, 192, 0, 0)                                                   \
-  X(7, 4, 224, 0, 0) X(7, 5, 288, 0, 0)                                                   \
-  X(8, 4, 256, 0, 0) X(8, 3, 160, 0, 0)
+// sized for (0: as many as the shared memory allows, up to 3), item mapping (0: one
+// thread per (element, line) in order, threads >= (edge + 1)^2 (degree + 1); 1:
+// warp-aligned, 32 / (degree + 1) whole elements per warp, whose three element phases
+// synchronise within the warp, threads = 32 x warps)).  Degree 4: 7x7 with one owned
+// buffer kept at 2 CTAs per SM (92 registers) is the fastest in order mapping; sized for
+// 3 CTAs it is capped at 64 registers and runs slower.  The two-float mode uses the same
+// list with one owned buffer.  New configurations go at the end of their degree's list:
+// the autotuner's cache refers to them by position.
+#define SE2P_CONFIGS(X)                                                                               \
+  X(1, 15, 512, 0, 0, 0) X(1, 11, 288, 0, 0, 0) X(1, 15, 512, 0, 0, 1)                                \
+  X(2, 12, 512, 2, 2, 0) X(2, 10, 384, 0, 0, 0) X(2, 8, 256, 0, 0, 0) X(2, 10, 416, 0, 0, 1)           \
+  X(3, 7, 256, 0, 0, 0) X(3, 8, 352, 0, 0, 0) X(3, 7, 256, 0, 0, 1)                                    \
+  X(4, 7, 320, 1, 2, 0) X(4, 7, 320, 2, 0, 0) X(4, 6, 256, 2, 0, 0) X(4, 8, 416, 0, 0, 0)              \
+  X(4, 7, 352, 1, 2, 1) X(4, 6, 288, 2, 0, 1)                                                          \
+  X(5, 6, 320, 0, 0, 0) X(5, 5, 224, 0, 0, 0) X(5, 6, 320, 0, 0, 1)                                    \
+  X(6, 5, 256, 0, 0, 0) X(6, 4, 192, 0, 0, 0) X(6, 5, 288, 0, 0, 1)                                    \
+  X(7, 4, 224, 0, 0, 0) X(7, 5, 288, 0, 0, 0) X(7, 4, 224, 0, 0, 1)                                    \
+  X(8, 4, 256, 0, 0, 0) X(8, 3, 160, 0, 0, 0) X(8, 4, 288, 0, 0, 1)
 
 // arithmetic modes of the persistent step kernel
 enum { MODE_PLAIN = 0, MODE_KAHAN = 1, MODE_DF = 2 };

@@ -1,5 +1,9 @@
 """Surrogate pipeline pieces that need the GPU: solver traces of mirrored
-problems (the augmentation's premise) and a short end-to-end train/predict."""
+problems (the augmentation's premise), a short end-to-end train/predict, and what
+a trained network gains over the method without it (the coarse-solver ladder) at
+equal misfit."""
+import time
+
 import numpy as np
 import pytest
 
@@ -76,3 +80,32 @@ def test_inference_copies_predict_the_same():
     a = SU.predict([net], data, np.arange(6))            # passes of 4 + 2
     b = SU.predict(big, data, np.arange(6))              # one pass of 6
     assert np.array_equal(a, b)
+
+
+def test_trained_network_beats_the_solver_ladder_at_equal_misfit():
+    """The learned part against the method without it: a network trained by the project's
+    own kernels (2400 draws and their mirrors, 16 epochs) predicts 64 held-out draws faster
+    than the fastest coarse solver of the ladder whose mean misfit is at most the
+    network's, against that solver's wall time and against its device time alone."""
+    tr = SU.generate(41, 2400)
+    te = SU.generate(42, 64)
+    dtrain = SU.DeviceData(tr, augment=True)
+    dtest = SU.DeviceData(te, scale=dtrain.scale)
+    rec_x = SU.receiver_cells(tr.specs[0])
+    net, st = SU.train(dtrain, np.arange(dtrain.n), rec_x, seed=0, epochs=16, batch=32, lr=1e-3)
+    assert st["loss"][-1] < 0.7 * st["loss"][0]
+    inf = SU.for_inference([net], 64)
+    SU.predict(inf, dtest, np.arange(8))           # warm: streams and buffers
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    preds = SU.predict(inf, dtest, np.arange(dtest.n))
+    secs = time.perf_counter() - t0
+    mis = float(SU.rel_l2(preds[0], te.traces).mean())
+    lad = SU.solver_ladder(te.specs, te.traces)
+    eq = SU.equal_misfit(lad, mis, dtest.n / secs)
+    print(f"network misfit {mis:.3f}, {dtest.n / secs:.0f} draws/s; fastest solver at most as wrong: "
+          f"{eq['solver'] and (eq['solver']['mx'], eq['solver']['p'], round(eq['solver']['misfit_mean'], 3), round(eq['solver']['draws_per_s']))}; "
+          f"gain {eq['gain']}, against its device time {eq['gain_solver_time']}")
+    assert 0.0 < mis < 1.0
+    assert eq["solver"] is not None, lad
+    assert eq["gain"] > 1.0 and eq["gain_solver_time"] > 1.0, eq
