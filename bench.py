@@ -641,12 +641,14 @@ def run_surrogate(args):
         what_if.append({"threshold": th, "fallback_rate": float(1 - acc.mean()),
                         "accepted_misfit_max": float(mis[acc].max()) if acc.any() else None,
                         "accepted_misfit_mean": float(mis[acc].mean()) if acc.any() else None})
-    served = SU.serve(inf, dtest, test.specs, threshold=args.threshold, audit=0.05)
+    served = SU.serve(inf, dtest, test.specs, threshold=args.threshold, audit=0.05, batch_requests=args.serve_batch)
     solver_sps = dtest.n / test.wall_seconds
-    # the gain at equal misfit: coarser solvers on the in-distribution held-out draws
-    ladder = SU.solver_ladder(te_in.specs, te_in.traces)
+    # the gain at equal misfit: coarser solvers on (the first --ladder-draws of) the
+    # in-distribution held-out draws, against the network's misfit on the same draws
+    nl = min(len(te_in), args.ladder_draws)
+    ladder = SU.solver_ladder(te_in.specs[:nl], te_in.traces[:nl])
     sur_sps = dtest.n / t_pred
-    eq = SU.equal_misfit(ladder, float(mis[~is_ood].mean()), sur_sps)
+    eq = SU.equal_misfit(ladder, float(mis[:nl].mean()), sur_sps)
     log(f"equal misfit: {eq}")
     line = {"metric": "seismograms/s surrogate vs solver @1% L2", "value": served["seismograms_per_s"],
             "unit": "seismograms/s", "n_gpus": 1, "higher_is_better": True, "dtype": "bf16", "data": "synthetic",
@@ -664,7 +666,7 @@ def run_surrogate(args):
                          "disagreement_mean": float(dis[~is_ood].mean()), "ood_disagreement_mean": float(dis[is_ood].mean()),
                          "corr_disagreement_misfit": float(np.corrcoef(dis, mis)[0, 1])},
             "what_if": what_if,
-            "equal_misfit": {"surrogate_misfit_mean": float(mis[~is_ood].mean()),
+            "equal_misfit": {"draws": nl, "surrogate_misfit_mean": float(mis[:nl].mean()),
                              "surrogate_draws_per_s": sur_sps, "fine_solver_draws_per_s": solver_sps,
                              "solver_ladder": ladder, "solver_at_equal_misfit": eq["solver"],
                              "gain_at_equal_misfit": eq["gain"],
@@ -685,6 +687,7 @@ def run_nn_step(args):
     from se2dr_fork_gb300 import nn as N
     from se2dr_fork_gb300 import surrogate as SU
     torch.cuda.set_device(0)
+    N.set_tensor_path(0 if args.mma_only else (2 if args.tc_all else 1))
     cfg = SU.net_config(args.nn_batch)
     net = N.Network(cfg, seed=0)
     stream = torch.cuda.Stream()
@@ -715,11 +718,15 @@ def run_nn_step(args):
         peak, kind = 1900.0, "fallback"
     sps = args.steps * args.nn_batch / secs
     tf = 3 * fwd * sps / 1e12
+    paths = N.tensor_path_info()
     print(json.dumps({"metric": "surrogate training samples/s", "value": sps, "unit": "samples/s", "n_gpus": 1,
                       "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
                       "higher_is_better": True, "dtype": "bf16", "data": "synthetic",
                       "config": {"workload": "training step of the 4-layer, width-64, 16-mode operator on 128^2 "
-                                             f"cells, batch {args.nn_batch}", "flops_per_sample": 3 * fwd},
+                                             f"cells, batch {args.nn_batch}", "flops_per_sample": 3 * fwd,
+                                 "row_gemms": ("mma.sync" if args.mma_only else "tcgen05" if args.tc_all
+                                               else "tcgen05 for K > 64, mma.sync below")},
+                      "gemm_launches": paths,
                       "roofline": {"bound": "tensor", "achieved": tf, "peak": peak, "unit": "TFLOP/s",
                                    "frac": tf / peak, "peak_kind": kind, "traffic": None}}), flush=True)
 
@@ -752,8 +759,12 @@ def main():
     ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--threshold", type=float, default=0.01)
+    ap.add_argument("--serve-batch", type=int, default=250, help="requests per serving batch")
+    ap.add_argument("--ladder-draws", type=int, default=1000, help="held-out draws the coarse-solver ladder re-solves")
     ap.add_argument("--nn-step", action="store_true", help="time the surrogate's training step alone")
     ap.add_argument("--nn-batch", type=int, default=32)
+    ap.add_argument("--mma-only", action="store_true", help="surrogate GEMMs on the mma.sync kernel only")
+    ap.add_argument("--tc-all", action="store_true", help="every qualifying surrogate row GEMM on tcgen05")
     ap.add_argument("--accuracy", action="store_true",
                     help="FP32 modes against FP64 over --steps steps (error table) instead of the headline run")
     args = ap.parse_args()

@@ -59,7 +59,7 @@ def build_host(force: bool = False) -> str:
 
 
 NN_UNITS = ["se2nn"]
-NN_DEPS = ["se2nn_gemm.cuh"]
+NN_DEPS = ["se2nn_gemm.cuh", "se2nn_tc.cuh"]
 
 
 def build_gpu(force: bool = False) -> str:

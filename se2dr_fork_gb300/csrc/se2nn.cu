@@ -17,6 +17,7 @@
 
 #include "se2nn.h"
 #include "se2nn_gemm.cuh"
+#include "se2nn_tc.cuh"
 
 using nnk::bf16;
 using nnk::GemmArgs;
@@ -375,9 +376,60 @@ GemmArgs mk(const bf16 *A, long lda, long sA, int tA, const bf16 *B, long ldb, l
   return g;
 }
 
+// ---- the tensor-core (tcgen05) path for the row GEMMs -----------------------------
+// 0: every GEMM runs gemm_bf16; 1 (default): qualifying row GEMMs with K > 64 run gemm_tc
+// (where it measured faster: the decoder's K = 128 GEMMs); 2: every qualifying row GEMM
+// runs gemm_tc
+int g_tc_path = 1;
+long g_tc_launches = 0, g_mma_launches = 0;
+__device__ int g_tc_err;
+
+bool tc_eligible(const GemmArgs &g)
+{
+  return g_tc_path && (g_tc_path == 2 || g.K > 64) && !g.transA && g.batch == 1 && g.M >= nnk::TC_M && g.K % 16 == 0 && g.K >= 16 &&
+         g.K <= nnk::TC_KMAX && g.N % 16 == 0 && g.N >= 16 && g.N <= nnk::TC_NMAX && g.lda % 8 == 0 &&
+         (reinterpret_cast<uintptr_t>(g.A) & 15) == 0;
+}
+
+cudaError_t launch_gemm_tc(const GemmArgs &g, cudaStream_t st)
+{
+  static int *err = nullptr;
+  static int nsm = 0;
+  static bool attr = false;
+  if (!err) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaGetSymbolAddress((void **)&err, g_tc_err);
+    if (e != cudaSuccess) return e;
+  }
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(nnk::gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)nnk::tc_smem_bytes(nnk::TC_NMAX, nnk::TC_KMAX));
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  // resident CTAs per SM: what registers and shared memory allow, capped by the 512
+  // tensor-memory columns of an SM (a CTA beyond them would wait in its allocation)
+  const size_t smem = nnk::tc_smem_bytes(g.N, g.K);
+  int occ = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, nnk::gemm_tc, nnk::TC_THREADS, smem) != cudaSuccess) {
+    cudaGetLastError();
+    occ = 1;
+  }
+  occ = std::max(1, std::min(occ, 512 / nnk::tc_tmem_cols(g.N)));
+  const int ntiles = (g.M + nnk::TC_M - 1) / nnk::TC_M;
+  const int grid = std::min(ntiles, occ * nsm);
+  nnk::gemm_tc<<<grid, nnk::TC_THREADS, smem, st>>>(g, err);
+  g_tc_launches++;
+  return cudaGetLastError();
+}
+
 cudaError_t launch_gemm(const GemmArgs &g, cudaStream_t st)
 {
   if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return cudaSuccess;
+  if (tc_eligible(g)) return launch_gemm_tc(g, st);
+  g_mma_launches++;
   const unsigned gy = (unsigned)((g.M + nnk::GBM - 1) / nnk::GBM), gx = (unsigned)((g.N + nnk::GBN - 1) / nnk::GBN);
   if (gy > 65535u || g.batch > 65535) return cudaErrorInvalidConfiguration;
   nnk::gemm_bf16<<<dim3(gx, gy, (unsigned)g.batch), nnk::GTHREADS, 0, st>>>(g);
@@ -774,6 +826,27 @@ extern "C" int se2nn_gather_targets(se2nn *h, const float *targets_dev, const in
   const long row = (long)h->c.nrec * h->c.nout;
   k_gather_rows<<<nblk(batch * row), EW, 0, h->stream>>>(targets_dev, idx_dev, batch, row, out_dev);
   NCK(h, cudaGetLastError());
+  return 0;
+}
+
+extern "C" int se2nn_set_tensor_path(int mode)
+{
+  if (mode < 0 || mode > 2) return -1;
+  g_tc_path = mode;
+  return 0;
+}
+
+extern "C" int se2nn_tensor_path_info(long out[3])
+{
+  if (!out) return -1;
+  int flag = 0;
+  if (cudaMemcpyFromSymbol(&flag, g_tc_err, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    return -2;
+  }
+  out[0] = g_tc_launches;
+  out[1] = g_mma_launches;
+  out[2] = flag;
   return 0;
 }
 

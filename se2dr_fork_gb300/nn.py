@@ -21,7 +21,8 @@ vp = C.c_void_p
 
 EXPORTS = ["se2nn_create", "se2nn_destroy", "se2nn_last_error", "se2nn_set_stream", "se2nn_num_params",
            "se2nn_get_params", "se2nn_set_params", "se2nn_get_grads", "se2nn_set_receivers", "se2nn_forward",
-           "se2nn_loss_grad", "se2nn_adam_step", "se2nn_build_inputs", "se2nn_gather_targets", "se2nn_gemm"]
+           "se2nn_loss_grad", "se2nn_adam_step", "se2nn_build_inputs", "se2nn_gather_targets", "se2nn_gemm",
+           "se2nn_set_tensor_path", "se2nn_tensor_path_info"]
 
 
 class CConfig(C.Structure):
@@ -77,12 +78,29 @@ def lib():
         L.se2nn_gather_targets.argtypes = [vp, vp, vp, C.c_int, vp]
         L.se2nn_gemm.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_long, C.c_long, C.c_long,
                                  C.c_long, C.c_long, C.c_long, C.c_int, C.c_int, C.c_float, C.c_float, vp]
+        L.se2nn_set_tensor_path.argtypes = [C.c_int]
+        L.se2nn_tensor_path_info.argtypes = [C.POINTER(C.c_long)]
         _lib = L
     return _lib
 
 
 class NnError(RuntimeError):
     pass
+
+
+def set_tensor_path(mode: int):
+    """Which GEMMs run on the tcgen05 tensor-core kernel (process-wide): 0 none (every GEMM on
+    the mma.sync kernel), 1 the row GEMMs with K > 64 (default), 2 every qualifying row GEMM."""
+    if lib().se2nn_set_tensor_path(int(mode)) != 0:
+        raise NnError(f"tensor path mode {mode} is not 0, 1 or 2")
+
+
+def tensor_path_info() -> dict:
+    """GEMM launches so far by kernel, and whether a tcgen05 GEMM's bounded wait expired."""
+    out = (C.c_long * 3)()
+    if lib().se2nn_tensor_path_info(out) != 0:
+        raise NnError("se2nn_tensor_path_info failed")
+    return {"tcgen05_launches": int(out[0]), "mma_sync_launches": int(out[1]), "wait_expired": bool(out[2])}
 
 
 def _ptr(t) -> int:

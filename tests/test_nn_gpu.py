@@ -74,6 +74,42 @@ def test_gemm_shared_operand_batches():
     assert rel(Cd.cpu().numpy(), np.einsum("mk,bkn->bmn", A, B)) < 1e-5
 
 
+@pytest.mark.parametrize("M,N_,K,tB,pad", [(128, 16, 16, 0, 0), (1000, 64, 64, 0, 8), (1000, 64, 64, 1, 0),
+                                            (16384, 64, 64, 0, 0), (4096, 128, 128, 1, 8), (777, 16, 128, 0, 0),
+                                            (2048, 128, 64, 0, 0)])
+def test_gemm_tensor_core_path_matches_numpy_and_mma(M, N_, K, tB, pad):
+    """Row GEMMs that qualify for the tcgen05 kernel (one batch, k-contiguous A, M >= 128,
+    K and N multiples of 16 up to 128, ragged row tiles included; mode 2 sends every one
+    there) agree with numpy and
+    with the mma.sync kernel to FP32 accumulation error; the launch counters show which
+    kernel ran, and no bounded wait expired."""
+    rng = np.random.default_rng(M + 3 * N_ + 7 * K + tB)
+    lda = K + pad
+    rb, cb = (N_, K) if tB else (K, N_)
+    ldb = cb + pad
+    A = bf16_round(rng.standard_normal((M, lda)))
+    B = bf16_round(rng.standard_normal((rb, ldb)))
+    C0 = rng.standard_normal((M, N_))
+    Ad, Bd = dev_bf16(A), dev_bf16(B)
+    opB = B[:, :cb].T if tB else B[:, :cb]
+    ref = 1.5 * (A[:, :K] @ opB) + 0.5 * C0.astype(np.float32)
+    out = {}
+    for tc in (True, False):
+        N.set_tensor_path(2 if tc else 0)
+        before = N.tensor_path_info()
+        Cd = torch.tensor(C0, dtype=torch.float32).cuda()
+        N.gemm(Ad, Bd, Cd, M, N_, K, 1, lda, ldb, N_, 0, 0, 0, 0, tB, alpha=1.5, beta=0.5)
+        torch.cuda.synchronize()
+        after = N.tensor_path_info()
+        key = "tcgen05_launches" if tc else "mma_sync_launches"
+        assert after[key] == before[key] + 1, (before, after)
+        out[tc] = Cd.cpu().numpy()
+    N.set_tensor_path(1)
+    assert not N.tensor_path_info()["wait_expired"]
+    assert rel(out[True], ref) < 1e-5, rel(out[True], ref)
+    assert rel(out[True], out[False]) < 1e-5
+
+
 def run_case(cfg, rec_x, B, seed):
     net = N.Network(cfg, seed=seed)
     net.set_receivers(rec_x)
