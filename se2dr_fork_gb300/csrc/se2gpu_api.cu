@@ -405,13 +405,15 @@ static int upload_leapfrog(se2gpu_solver *h, const double *u, const double *v, c
 
 // select one of the persistent kernel's tile configurations: kernel attributes,
 // tensor-map boxes, per-tile source/receiver lists and the persistent grid
-static int setup_f32_config(se2gpu_solver *h, int config)
+// (in_create: the handle has run no step yet, so nothing in flight reads the tile lists
+// and the host work here overlaps the set-up kernels still reading the caller's arrays)
+static int setup_f32_config(se2gpu_solver *h, int config, bool in_create = false)
 {
   const bool kahan = is_kahan(h);
   const int mode = pmode(h);
   se2p::TileShape ts;
   if (se2p::config_shape(h->p, config, mode, &ts)) return fail(h, SE2GPU_ERR_ARG, "no tile configuration %d for degree %d", config, h->p);
-  CK(h, cudaStreamSynchronize(h->stream));
+  if (!in_create) CK(h, cudaStreamSynchronize(h->stream));
   {
     cudaError_t e = se2p::prepare(h->p, config, mode);
     if (e != cudaSuccess) return fail(h, SE2GPU_ERR_CUDA, "persistent kernel set-up: %s", cudaGetErrorString(e));
@@ -574,6 +576,15 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
       TRY(dzero(h, (void **)&h->rbuf[b], (size_t)P->nrec * npe * rbuf_values(h) * 4));
     }
     TRY(dalloc(h, (void **)&h->pa, np * 8 * (df ? 2 : 1)));   // two-float mode: low parts after the high
+    // the step kernel's tables and tile configuration first: their small uploads then wait
+    // only for the cell tables above, not for the clearing and the 1/M pass below
+    {
+      cudaError_t e = se2p::set_tables(P->p, P->D, P->w1d);
+      if (e != cudaSuccess) { fail(h, SE2GPU_ERR_CUDA, "constant tables: %s", cudaGetErrorString(e)); TRY(SE2GPU_ERR_CUDA); }
+      h->src_elem_h = new std::vector<int>(P->src_elem, P->src_elem + P->nsrc);
+      h->rec_elem_h = new std::vector<int>(P->rec_elem, P->rec_elem + P->nrec);
+      TRY(setup_f32_config(h, 0, true));
+    }
     // The fields start at zero: the first buffer set and a are cleared.  The second set is
     // written at every mesh node by the first step before anything reads it (the tile copies
     // never read past the mesh), so only its row padding is cleared, to keep checkpoints
@@ -642,13 +653,6 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
       });
       TRY(dalloc(h, (void **)&h->pminv, nm * 4));
       if (cudaMemcpyAsync(h->pminv, minv.get(), nm * 4, cudaMemcpyHostToDevice, h->stream) != cudaSuccess) { fail(h, SE2GPU_ERR_CUDA, "upload 1/M"); TRY(SE2GPU_ERR_CUDA); }
-    }
-    {
-      cudaError_t e = se2p::set_tables(P->p, P->D, P->w1d);
-      if (e != cudaSuccess) { fail(h, SE2GPU_ERR_CUDA, "constant tables: %s", cudaGetErrorString(e)); TRY(SE2GPU_ERR_CUDA); }
-      h->src_elem_h = new std::vector<int>(P->src_elem, P->src_elem + P->nsrc);
-      h->rec_elem_h = new std::vector<int>(P->rec_elem, P->rec_elem + P->nrec);
-      TRY(setup_f32_config(h, 0));
     }
   }
   {
@@ -1105,6 +1109,7 @@ extern "C" int se2gpu_set_tile_config(se2gpu_solver *h, int config)
   if (is_f64(h)) return (config == 0) ? 0 : fail(h, SE2GPU_ERR_ARG, "FP64 mode has a single tile configuration");
   if (config < 0 || config >= se2p::num_configs(h->p)) return fail(h, SE2GPU_ERR_ARG, "tile configuration %d out of range", config);
   CK(h, cudaSetDevice(h->device));
+  if (config == h->pconfig) return 0;   // already selected: tables, maps and grid are current
   return setup_f32_config(h, config);
 }
 

@@ -619,13 +619,16 @@ __device__ __forceinline__ tf tf_add(tf a, tf b)
   const tf s = tf_two_sum(a.h, b.h);
   return tf_fast_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
 }
+// the product as the pair (rounded product, remainder), not renormalised: the remainder
+// is within about two units in the last place of the product, and every consumer (another
+// product, a sum, a dot-product term) takes a pair in that state at the same accuracy
 __device__ __forceinline__ tf tf_mul(tf a, tf b)
 {
   const float p = __fmul_rn(a.h, b.h);
   float e = __fmaf_rn(a.h, b.h, -p);
   e = __fmaf_rn(a.h, b.l, e);
   e = __fmaf_rn(a.l, b.h, e);
-  return tf_fast_sum(p, e);
+  return tf{p, e};
 }
 __device__ __forceinline__ tf tf_neg(tf a) { return tf{-a.h, -a.l}; }
 // s += a * x, unnormalised (Dot2 step); finish with tf_norm

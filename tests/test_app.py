@@ -36,6 +36,32 @@ def test_app_matches_reference_executable(app, name, tmp_path):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("name", ["cli_demo_default", "cli_demo_6x4_p3"])
+def test_app_fp32_df_receiver_file_matches_reference_values(app, name, tmp_path):
+    """With -precision fp32_df the application's receiver file carries the reference's
+    values to the 9 significant digits it prints (within 1e-7 of each trace's largest
+    value), with the same header and rows."""
+    g = load(name)
+    args = [str(a) for a in g["args"]] + ["-precision", "fp32_df"]
+    r = subprocess.run([app, *args], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    for key in g:
+        if key.startswith("name_") and str(g[key]).endswith(".dat"):
+            fname = str(g[key])
+            ref_text = str(g["file_" + key[5:]])
+            got_text = open(tmp_path / fname).read()
+            ref_head = [l for l in ref_text.splitlines() if l.startswith("#")]
+            got_head = [l for l in got_text.splitlines() if l.startswith("#")]
+            assert got_head == ref_head
+            ref = np.array([[float(v) for v in l.split()] for l in ref_text.splitlines() if l and not l.startswith("#")])
+            got = np.array([[float(v) for v in l.split()] for l in got_text.splitlines() if l and not l.startswith("#")])
+            assert got.shape == ref.shape
+            assert np.array_equal(got[:, 0], ref[:, 0])
+            scale = np.maximum(np.abs(ref[:, 1:]).max(axis=0), 1e-300)
+            assert np.max(np.abs(got[:, 1:] - ref[:, 1:]) / scale) < 1e-7
+
+
+@pytest.mark.gpu
 def test_app_fp32_kahan_runs(app, tmp_path):
     r = subprocess.run([app, "-mx", "16", "-bdegree", "4", "-precision", "fp32_kahan", "-tmax", "0.2"], cwd=tmp_path,
                        capture_output=True, text=True, timeout=300)
