@@ -341,11 +341,15 @@ def run_ours(args, rank, world):
             sol.set_tile_config(args.tile_config)
         else:
             autotune.apply(sol, prec)
+    t_create = time.perf_counter()
     sol.advance(args.steps)
     tr = sol.traces()
+    t_steps = time.perf_counter()
     sol.close()
     torch.cuda.synchronize()
-    e2e_s = tmax(time.perf_counter() - t0)
+    t_end = time.perf_counter()
+    e2e_s = tmax(t_end - t0)
+    e2e_parts = {"create_s": t_create - t0, "steps_and_traces_s": t_steps - t_create, "destroy_s": t_end - t_steps}
     # bytes of the caller's FP64 host arrays that se2gpu_create and advance read: the mass, the
     # cell Lame parameters, the Jacobians, D and the weights, the source values, the receiver
     # indices and the STF values of every step (the FP32 modes convert on the device)
@@ -382,7 +386,7 @@ def run_ours(args, rank, world):
             "roofline": head["roofline"], "clocks": head["clocks"], "gpu_launches": head["launches"],
             "tile": head.get("tile"), "autotune": tuned,
             "e2e": {"value": world * dof * args.steps / e2e_s, "unit": "DOF/s", "h2d_bytes_per_step": h2d / args.steps,
-                    "d2h_bytes_per_step": d2h / args.steps, "seconds": e2e_s,
+                    "d2h_bytes_per_step": d2h / args.steps, "seconds": e2e_s, "parts": e2e_parts,
                     "includes": "se2gpu_create (upload of the set-up from host memory), advance, traces, destroy"},
             "cpu_baseline": cpu}
     for leg in ("fp64", "fp32_df"):
@@ -459,12 +463,16 @@ def run_accuracy(args):
     k_shear = 2.0 * np.pi * 8.0 / (5000.0 / 1.73)   # Ricker f0 over the mean shear speed
     for p, mx in cases:
         vp = H.gaussian_random_field(mx, mx, 5000.0, 0.1, 8.0, seed=2048)
-        setup = H.Setup(S.grf2048(mx, mx, p=p, nt=args.steps, cells=(vp, vp / 1.73, np.full_like(vp, 2700.0))))
+        cells = (vp, vp / 1.73, np.full_like(vp, 2700.0))
+        steps = args.steps
+        if args.acc_tmax > 0:   # as many steps as reach this time on this mesh
+            steps = int(np.ceil(args.acc_tmax / H.Setup(S.grf2048(mx, mx, p=p, nt=1, cells=cells)).dt))
+        setup = H.Setup(S.grf2048(mx, mx, p=p, nt=steps, cells=cells))
         ref = None
         for prec in ["fp64", "fp32_df", "fp32_kahan", "fp32"]:
-            sol = G.Solver(setup, prec, trace_capacity=min(args.steps, 2000))
+            sol = G.Solver(setup, prec, trace_capacity=min(steps, 2000))
             t0 = time.time()
-            tr = sol.run(args.steps, block=2000)
+            tr = sol.run(steps, block=2000)
             sol.synchronize()
             secs = time.time() - t0
             fields = sol.fields()
@@ -476,7 +484,7 @@ def run_accuracy(args):
                 errs = trace_errors(tr, ref[0], k_shear)
                 ferr = {n: float(np.linalg.norm(x - y) / np.linalg.norm(y)) for n, x, y in zip("uva", fields, ref[1])}
             print(json.dumps({"accuracy": "sweep" if args.sweep else "grf2048", "p": p, "mx": mx, "nodes": setup.nnodes,
-                              "steps": args.steps, "t_end": float(tr[-1, 0]) if len(tr) else 0.0,
+                              "steps": steps, "t_end": float(tr[-1, 0]) if len(tr) else 0.0,
                               "receivers": setup.nrec, "precision": prec, "wall_s": secs,
                               "trace_rel_l2": dict(zip(["ux", "uy", "vx", "vy", "ax", "ay", "curl"], errs)) if errs else None,
                               "field_rel_l2": ferr}), flush=True)
@@ -767,6 +775,8 @@ def main():
     ap.add_argument("--tc-all", action="store_true", help="every qualifying surrogate row GEMM on tcgen05")
     ap.add_argument("--accuracy", action="store_true",
                     help="FP32 modes against FP64 over --steps steps (error table) instead of the headline run")
+    ap.add_argument("--acc-tmax", type=float, default=0.0,
+                    help="with --accuracy: run each mesh to this time instead of --steps steps")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
