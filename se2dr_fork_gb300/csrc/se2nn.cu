@@ -8,6 +8,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <mutex>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -380,8 +382,8 @@ GemmArgs mk(const bf16 *A, long lda, long sA, int tA, const bf16 *B, long ldb, l
 // 0: every GEMM runs gemm_bf16; 1 (default): qualifying row GEMMs with K > 64 run gemm_tc
 // (where it measured faster: the decoder's K = 128 GEMMs); 2: every qualifying row GEMM
 // runs gemm_tc
-int g_tc_path = 1;
-long g_tc_launches = 0, g_mma_launches = 0;
+std::atomic<int> g_tc_path{1};
+std::atomic<long> g_tc_launches{0}, g_mma_launches{0};
 __device__ int g_tc_err;
 
 bool tc_eligible(const GemmArgs &g)
@@ -391,24 +393,40 @@ bool tc_eligible(const GemmArgs &g)
          (reinterpret_cast<uintptr_t>(g.A) & 15) == 0;
 }
 
+// per device (the current one at the launch): the error flag's address, the SM count and
+// the kernel's shared-memory limit, set up on the first launch on that device
+struct TcDevice {
+  int *err = nullptr;
+  int nsm = 0;
+};
+
 cudaError_t launch_gemm_tc(const GemmArgs &g, cudaStream_t st)
 {
-  static int *err = nullptr;
-  static int nsm = 0;
-  static bool attr = false;
-  if (!err) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = cudaGetSymbolAddress((void **)&err, g_tc_err);
-    if (e != cudaSuccess) return e;
+  static std::mutex mu;
+  static TcDevice devs[64];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  TcDevice d;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!devs[dev].err) {
+      int nsm = 0;
+      int *err = nullptr;
+      e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      if (e == cudaSuccess) e = cudaGetSymbolAddress((void **)&err, g_tc_err);
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(nnk::gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)nnk::tc_smem_bytes(nnk::TC_NMAX, nnk::TC_KMAX));
+      if (e != cudaSuccess) return e;
+      devs[dev].nsm = nsm;
+      devs[dev].err = err;
+    }
+    d = devs[dev];
   }
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(nnk::gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)nnk::tc_smem_bytes(nnk::TC_NMAX, nnk::TC_KMAX));
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  int *err = d.err;
+  const int nsm = d.nsm;
   // resident CTAs per SM: what registers and shared memory allow, capped by the 512
   // tensor-memory columns of an SM (a CTA beyond them would wait in its allocation)
   const size_t smem = nnk::tc_smem_bytes(g.N, g.K);
@@ -839,13 +857,13 @@ extern "C" int se2nn_set_tensor_path(int mode)
 extern "C" int se2nn_tensor_path_info(long out[3])
 {
   if (!out) return -1;
-  int flag = 0;
+  int flag = 0;   // (the current device's flag)
   if (cudaMemcpyFromSymbol(&flag, g_tc_err, sizeof(int)) != cudaSuccess) {
     cudaGetLastError();
     return -2;
   }
-  out[0] = g_tc_launches;
-  out[1] = g_mma_launches;
+  out[0] = g_tc_launches.load();
+  out[1] = g_mma_launches.load();
   out[2] = flag;
   return 0;
 }
