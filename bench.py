@@ -733,7 +733,7 @@ def run_nn_step(args):
                       "config": {"workload": "training step of the 4-layer, width-64, 16-mode operator on 128^2 "
                                              f"cells, batch {args.nn_batch}", "flops_per_sample": 3 * fwd,
                                  "row_gemms": ("mma.sync" if args.mma_only else "tcgen05" if args.tc_all
-                                               else "tcgen05 for K > 64, mma.sync below")},
+                                               else "tcgen05 except the 1x1 convolutions' shape")},
                       "gemm_launches": paths,
                       "roofline": {"bound": "tensor", "achieved": tf, "peak": peak, "unit": "TFLOP/s",
                                    "frac": tf / peak, "peak_kind": kind, "traffic": None}}), flush=True)

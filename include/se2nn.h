@@ -97,8 +97,8 @@ int se2nn_gemm(const void *A_dev, const void *B_dev, float *C_dev, int M, int N,
    lift, the 1x1 convolutions, the decoder and their data gradients -- can run on the
    5th-generation tensor cores (tcgen05.mma, accumulators in tensor memory), the others
    run on the mma.sync kernel.  mode 0: every GEMM on mma.sync; 1 (default): the row
-   GEMMs with K > 64 on tcgen05 (the shapes where it measured faster); 2: every row GEMM
-   on tcgen05.  Process-wide.  se2nn_tensor_path_info: out[0] = tcgen05 GEMM launches,
+   GEMMs on tcgen05 except those with N <= 64 and 32 < K <= 64 (the 1x1 convolutions,
+   where mma.sync measured faster); 2: every row GEMM on tcgen05.  Process-wide.  se2nn_tensor_path_info: out[0] = tcgen05 GEMM launches,
    out[1] = mma.sync GEMM launches, out[2] = 1 if a tcgen05 GEMM's bounded wait ever
    expired. */
 int se2nn_set_tensor_path(int mode);

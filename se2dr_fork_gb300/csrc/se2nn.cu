@@ -379,16 +379,16 @@ GemmArgs mk(const bf16 *A, long lda, long sA, int tA, const bf16 *B, long ldb, l
 }
 
 // ---- the tensor-core (tcgen05) path for the row GEMMs -----------------------------
-// 0: every GEMM runs gemm_bf16; 1 (default): qualifying row GEMMs with K > 64 run gemm_tc
-// (where it measured faster: the decoder's K = 128 GEMMs); 2: every qualifying row GEMM
-// runs gemm_tc
+// 0: every GEMM runs gemm_bf16; 1 (default): qualifying row GEMMs run gemm_tc except those
+// with N <= 64 and 32 < K <= 64 (the 1x1 convolutions and their data gradients, where
+// the mma.sync kernel measured faster); 2: every qualifying row GEMM runs gemm_tc
 std::atomic<int> g_tc_path{1};
 std::atomic<long> g_tc_launches{0}, g_mma_launches{0};
 __device__ int g_tc_err;
 
 bool tc_eligible(const GemmArgs &g)
 {
-  return g_tc_path && (g_tc_path == 2 || g.K > 64) && !g.transA && g.batch == 1 && g.M >= nnk::TC_M && g.K % 16 == 0 && g.K >= 16 &&
+  return g_tc_path && (g_tc_path == 2 || !(g.N <= 64 && g.K > 32 && g.K <= 64)) && !g.transA && g.batch == 1 && g.M >= nnk::TC_M && g.K % 16 == 0 && g.K >= 16 &&
          g.K <= nnk::TC_KMAX && g.N % 16 == 0 && g.N >= 16 && g.N <= nnk::TC_NMAX && g.lda % 8 == 0 &&
          (reinterpret_cast<uintptr_t>(g.A) & 15) == 0;
 }

@@ -13,16 +13,17 @@
 //  * op(B) (the layer's weights, N x K) is staged once per CTA in shared memory in the
 //    canonical K-major layout without swizzle: 8 x 8 core matrices of 128 bytes, the
 //    core matrix (row group g, k chunk c) at byte ((g * K/8) + c) * 128;
-//  * the A tiles (128 x K) are copied with 16-byte cp.async into the same layout, three
-//    stages (two tiles ahead) for K <= 64, two above;
+//  * the A tiles (128 x K) are copied with 16-byte cp.async into the same layout, two
+//    stages;
 //  * one thread issues K/16 tcgen05.mma (M = 128, N, K = 16, BF16 in, FP32 accumulate)
 //    per tile and commits them to the mbarrier of one of two tensor-memory accumulators;
 //    shared-memory descriptors: start address, leading byte offset 128 (the next k
 //    chunk), stride byte offset K/8 * 128 (the next row group).  The next tile's MMAs
 //    run while the current tile's epilogue reads the other accumulator;
 //  * eight warps read the accumulator, two per 32 lanes (rows), with tcgen05.ld
-//    32x32b.x16, alternate 16-column chunks each, and turn them through a per-warp shared-memory patch so that
-//    the epilogue's loads and stores run along rows (4 consecutive columns per lane).
+//    32x32b.x32, alternate 32-column chunks each, and turn them through a per-warp
+//    shared-memory patch so that the epilogue's loads and stores run along rows (4
+//    consecutive columns per lane, whole 128-byte row segments per chunk).
 // Every mbarrier wait is bounded: on expiry the kernel raises *err, waits (bounded) for
 // its own tensor-core operations, frees its tensor memory and returns.
 #pragma once
@@ -38,10 +39,10 @@ constexpr int TC_M = 128, TC_THREADS = 256, TC_KMAX = 128, TC_NMAX = 128;
 constexpr long TC_WAIT_LIMIT = 1L << 18;   // about one second of polls
 
 // shared memory: B [N][K], the A stages [128][K] (canonical layouts), the epilogue
-// patches (8 warps x 32 rows x 17 floats), then two barriers and the tensor-memory address.
-// Three A stages (copies two tiles ahead) where K <= 64, two above.
-constexpr int TC_PATCH = 32 * 17;
-__host__ __device__ constexpr int tc_stages(int K) { return K <= 64 ? 3 : 2; }
+// patches (8 warps x 32 rows x 33 floats), then two barriers and the tensor-memory address.
+// Two A stages (a third, copying two tiles ahead, measured no faster).
+constexpr int TC_PATCH = 32 * 33;   // 32 rows x 32 columns, padded
+__host__ __device__ constexpr int tc_stages(int) { return 2; }
 __host__ __device__ constexpr size_t tc_smem_bytes(int N, int K)
 {
   return (size_t)N * K * 2 + tc_stages(K) * (size_t)TC_M * K * 2 + (TC_THREADS / 32) * TC_PATCH * 4 + 64;
@@ -104,6 +105,24 @@ __device__ __forceinline__ void tc_commit(uint32_t bar)
 }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 32 consecutive FP32 accumulator columns of this thread's lane
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float *v)
+{
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
 
 // 16 consecutive FP32 accumulator columns of this thread's lane
 __device__ __forceinline__ void tc_ld16(uint32_t taddr, float *v)
@@ -284,17 +303,24 @@ __global__ void __launch_bounds__(TC_THREADS, 2) gemm_tc(const GemmArgs g, int *
     const int quarter = warp & 3;
     const long row0 = (long)tile_of(i) * TC_M + quarter * 32;
     const uint32_t acc = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((i & 1) * acc_cols);
-    for (int n0 = (warp >> 2) * 16; n0 < N; n0 += 32) {
-      float v[16];
-      tc_ld16(acc + (uint32_t)n0, v);
+    // chunks of 32 columns (16 where N is not a multiple of 32), alternating between the
+    // two warps of a lane quarter; a chunk's row segments are then written whole (32
+    // floats = one 128-byte line), 4 consecutive columns per lane
+    const int CW = (N % 32 == 0) ? 32 : 16, LPR = CW / 4, RPP = 32 / LPR;   // lanes per row, rows per pass
+    for (int n0 = (warp >> 2) * CW; n0 < N; n0 += 2 * CW) {
+      {
+        float v[32];
+        if (CW == 32) tc_ld32(acc + (uint32_t)n0, v);
+        else tc_ld16(acc + (uint32_t)n0, v);
 #pragma unroll
-      for (int c = 0; c < 16; c++) pw[lane * 17 + c] = v[c];
+        for (int c = 0; c < 32; c++)
+          if (c < CW) pw[lane * 33 + c] = v[c];
+      }
       __syncwarp();
-#pragma unroll
-      for (int pass = 0; pass < 4; pass++) {
-        const int r = pass * 8 + (lane >> 2), c4 = (lane & 3) * 4;
+      for (int pass = 0; pass < 32 / RPP; pass++) {
+        const int r = pass * RPP + lane / LPR, c4 = (lane % LPR) * 4;
         const long m = row0 + r;
-        float x[4] = {pw[r * 17 + c4], pw[r * 17 + c4 + 1], pw[r * 17 + c4 + 2], pw[r * 17 + c4 + 3]};
+        float x[4] = {pw[r * 33 + c4], pw[r * 33 + c4 + 1], pw[r * 33 + c4 + 2], pw[r * 33 + c4 + 3]};
         if (m < g.M) tc_epilogue4(g, m, n0 + c4, x);
       }
       __syncwarp();

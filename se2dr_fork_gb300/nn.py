@@ -90,7 +90,8 @@ class NnError(RuntimeError):
 
 def set_tensor_path(mode: int):
     """Which GEMMs run on the tcgen05 tensor-core kernel (process-wide): 0 none (every GEMM on
-    the mma.sync kernel), 1 the row GEMMs with K > 64 (default), 2 every qualifying row GEMM."""
+    the mma.sync kernel), 1 the row GEMMs except the 1x1 convolutions' shape (N <= 64,
+    32 < K <= 64), where mma.sync measured faster (default), 2 every qualifying row GEMM."""
     if lib().se2nn_set_tensor_path(int(mode)) != 0:
         raise NnError(f"tensor path mode {mode} is not 0, 1 or 2")
 

@@ -76,7 +76,7 @@ def test_gemm_shared_operand_batches():
 
 @pytest.mark.parametrize("M,N_,K,tB,pad", [(128, 16, 16, 0, 0), (1000, 64, 64, 0, 8), (1000, 64, 64, 1, 0),
                                             (16384, 64, 64, 0, 0), (4096, 128, 128, 1, 8), (777, 16, 128, 0, 0),
-                                            (2048, 128, 64, 0, 0)])
+                                            (2048, 128, 64, 0, 0), (4096, 128, 16, 0, 8)])
 def test_gemm_tensor_core_path_matches_numpy_and_mma(M, N_, K, tB, pad):
     """Row GEMMs that qualify for the tcgen05 kernel (one batch, k-contiguous A, M >= 128,
     K and N multiples of 16 up to 128, ragged row tiles included; mode 2 sends every one
