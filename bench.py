@@ -54,11 +54,13 @@ def alg_bytes_per_node(precision: str, ne: int, nnodes: int) -> float:
     cell = ne / nnodes
     if precision == "fp64":
         return 2 * 3 * 16 + 8 + 16 * cell          # u,v,a (double2) in+out, M, (lambda, mu)
+    # the plain and Kahan kernels read a float4 of constants per cell (lambda detJ, mu detJ,
+    # d xi/dx, d eta/dy); the two-float kernel reads (lambda, mu) with their low parts
     if precision == "fp32_kahan":
-        return 2 * 4 * 8 + 4 + 8 * cell            # leapfrog u,w,cu,cw (float2) in+out, 1/M, (lambda, mu)
+        return 2 * 4 * 8 + 4 + 16 * cell           # leapfrog u,w,cu,cw (float2) in+out, 1/M, cell constants
     if precision == "fp32_df":
         return 2 * 4 * 8 + 8 + 16 * cell           # the same state, 1/M and (lambda, mu) with their low parts
-    return 2 * 2 * 8 + 4 + 8 * cell                # leapfrog u,w (float2) in+out, 1/M, (lambda, mu)
+    return 2 * 2 * 8 + 4 + 16 * cell               # leapfrog u,w (float2) in+out, 1/M, cell constants
 
 
 def fp64_ops_per_node(p: int) -> float:

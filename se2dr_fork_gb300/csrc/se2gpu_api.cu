@@ -291,6 +291,19 @@ __global__ void k_to_float(const double *__restrict__ src, size_t n, float *__re
   }
 }
 
+// the constants of each cell as the plain and Kahan step kernels use them, from the
+// float tables: (lam detJ, mu detJ, d xi/dx, d eta/dy), detJ = J00 J11, products rounded
+__global__ void k_cell_consts(const float *__restrict__ lam, const float *__restrict__ mu, const float *__restrict__ J00,
+                              const float *__restrict__ J11, const float *__restrict__ iJ00,
+                              const float *__restrict__ iJ11, int mx, long ne, float4 *__restrict__ out)
+{
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < ne; i += (long)gridDim.x * blockDim.x) {
+    const int ex = (int)(i % mx), ey = (int)(i / mx);
+    const float detJ = __fmul_rn(J00[ex], J11[ey]);
+    out[i] = make_float4(__fmul_rn(lam[i], detJ), __fmul_rn(mu[i], detJ), iJ00[ex], iJ11[ey]);
+  }
+}
+
 // upload an FP64 host array in the handle's compute precision (two-float mode: the n
 // nearest floats followed by the n remainders, rounded to float).  FP32 tables on a
 // device that reads pageable host memory are converted by a kernel on the handle's
@@ -349,7 +362,7 @@ extern "C" void se2gpu_destroy(se2gpu_solver *h)
   void *ptrs[] = {h->pa, h->pminv, h->mass_bad, h->err_dev, h->mass, h->lam, h->mu, h->J00, h->J11, h->iJ00, h->iJ11, h->D, h->wq,
                   h->src_vals, h->Dd, h->iJ00d, h->iJ11d, h->stf_dev, h->traces, h->norm_part, h->src_elem,
                   h->rec_node, h->rec_elem, h->rec_gll, h->scratch_u, h->scratch_f, h->tile_src_off,
-                  h->tile_src_idx, h->tile_rec_off, h->tile_rec_idx};
+                  h->tile_src_idx, h->tile_rec_off, h->tile_rec_idx, h->cellc, h->tile_bounds};
   for (void *p : ptrs) dfree(h, p);
   if (h->stream) cudaStreamSynchronize(h->stream);   // the frees are done before the stream goes
   delete h->src_elem_h;
@@ -403,6 +416,21 @@ static int upload_leapfrog(se2gpu_solver *h, const double *u, const double *v, c
   return 0;
 }
 
+// the step kernel's tensor maps of the per-tile constants (plain and Kahan modes): the
+// cell box and the 1/M box, the same for both buffer sets (the two-float mode reads its
+// constants with loads and has neither)
+static int make_const_maps(se2gpu_solver *h, const se2p::TileShape &ts)
+{
+  for (int b = 0; b < 2; b++) memset(&h->maps[b][4], 0, 2 * sizeof(CUtensorMap));
+  if (pmode(h) == se2p::MODE_DF) return 0;
+  int r = se2p::make_map_cells(&h->maps[0][4], h->cellc, h->mx, h->my, ts.cell_box);
+  if (!r) r = se2p::make_map_f32(&h->maps[0][5], h->pminv, h->pitch, h->ny_g, h->pitch, ts.minv_w, ts.own_h);
+  if (r) return fail(h, SE2GPU_ERR_CUDA, "cuTensorMapEncodeTiled failed for the tile constants (%d)", r);
+  h->maps[1][4] = h->maps[0][4];
+  h->maps[1][5] = h->maps[0][5];
+  return 0;
+}
+
 // select one of the persistent kernel's tile configurations: kernel attributes,
 // tensor-map boxes, per-tile source/receiver lists and the persistent grid
 // (in_create: the handle has run no step yet, so nothing in flight reads the tile lists
@@ -426,6 +454,10 @@ static int setup_f32_config(se2gpu_solver *h, int config, bool in_create = false
       if (r) return fail(h, SE2GPU_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", r);
     }
   }
+  if (h->pminv) {   // (in se2gpu_create the 1/M map follows once 1/M is allocated)
+    int r = make_const_maps(h, ts);
+    if (r) return r;
+  }
   const int te = ts.tex, P = h->p;
   const int ntx = (h->mx + te - 1) / te, nty = (h->my + te - 1) / te, ntiles = ntx * nty;
   // tile lists: a source or receiver element appears in every tile whose owned nodes it touches
@@ -448,9 +480,17 @@ static int setup_f32_config(se2gpu_solver *h, int config, bool in_create = false
   std::vector<int> so, si, ro, ri;
   build(*h->src_elem_h, so, si);
   build(*h->rec_elem_h, ro, ri);
+  std::vector<int> tb(4 * (size_t)ntiles);
+  for (int t = 0; t < ntiles; t++) {
+    tb[4 * (size_t)t] = so[t]; tb[4 * (size_t)t + 1] = so[t + 1];
+    tb[4 * (size_t)t + 2] = ro[t]; tb[4 * (size_t)t + 3] = ro[t + 1];
+  }
   dfree(h, h->tile_src_off); dfree(h, h->tile_src_idx); dfree(h, h->tile_rec_off); dfree(h, h->tile_rec_idx);
+  dfree(h, h->tile_bounds);
   h->tile_src_off = h->tile_src_idx = h->tile_rec_off = h->tile_rec_idx = nullptr;
+  h->tile_bounds = nullptr;
   int rc;
+  if ((rc = upload_i(h, (int **)&h->tile_bounds, tb.data(), tb.size()))) return rc;
   if ((rc = upload_i(h, &h->tile_src_off, so.data(), so.size()))) return rc;
   if ((rc = upload_i(h, &h->tile_src_idx, si.data(), si.size()))) return rc;
   if ((rc = upload_i(h, &h->tile_rec_off, ro.data(), ro.size()))) return rc;
@@ -576,6 +616,13 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
       TRY(dzero(h, (void **)&h->rbuf[b], (size_t)P->nrec * npe * rbuf_values(h) * 4));
     }
     TRY(dalloc(h, (void **)&h->pa, np * 8 * (df ? 2 : 1)));   // two-float mode: low parts after the high
+    if (!df) {
+      TRY(dalloc(h, (void **)&h->cellc, (size_t)ne * sizeof(float4)));
+      k_cell_consts<<<(int)std::min<long>((ne + 255) / 256, 8L * h->nsm), 256, 0, h->stream>>>(
+          (const float *)h->lam, (const float *)h->mu, (const float *)h->J00, (const float *)h->J11,
+          (const float *)h->iJ00, (const float *)h->iJ11, h->mx, ne, h->cellc);
+      if (cudaGetLastError() != cudaSuccess) { fail(h, SE2GPU_ERR_CUDA, "cell constants"); TRY(SE2GPU_ERR_CUDA); }
+    }
     // the step kernel's tables and tile configuration first: their small uploads then wait
     // only for the cell tables above, not for the clearing and the 1/M pass below
     {
@@ -654,6 +701,9 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
       TRY(dalloc(h, (void **)&h->pminv, nm * 4));
       if (cudaMemcpyAsync(h->pminv, minv.get(), nm * 4, cudaMemcpyHostToDevice, h->stream) != cudaSuccess) { fail(h, SE2GPU_ERR_CUDA, "upload 1/M"); TRY(SE2GPU_ERR_CUDA); }
     }
+    se2p::TileShape ts;
+    if (se2p::config_shape(h->p, h->pconfig, pmode(h), &ts)) { fail(h, SE2GPU_ERR_ARG, "tile configuration"); TRY(SE2GPU_ERR_ARG); }
+    TRY(make_const_maps(h, ts));
   }
   {
     // one wait for everything queued above (kernels that read the caller's arrays included),
@@ -759,6 +809,7 @@ static se2p::Params f32_params(se2gpu_solver *h)
   prm.err = h->err_dev;
   prm.tile_src_off = h->tile_src_off; prm.tile_src_idx = h->tile_src_idx;
   prm.tile_rec_off = h->tile_rec_off; prm.tile_rec_idx = h->tile_rec_idx;
+  prm.cellc = h->cellc; prm.tile_bounds = h->tile_bounds;
   return prm;
 }
 

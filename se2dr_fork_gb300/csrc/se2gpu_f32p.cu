@@ -33,14 +33,14 @@ struct Entry {
 template <int P, int TE, int NT, int NOB = owned_buffers(P), int MINB = 0, bool WE = false>
 static Entry entry()
 {
-  constexpr int M0 = MINB ? MINB : min_blocks(Layout<P, TE, false, NOB>::TOTAL);
-  constexpr int M1 = MINB ? MINB : min_blocks(Layout<P, TE, true, NOB>::TOTAL);
+  constexpr int M0 = MINB ? MINB : min_blocks(Layout<P, TE, false, NOB, false, true>::TOTAL);
+  constexpr int M1 = MINB ? MINB : min_blocks(Layout<P, TE, true, NOB, false, true>::TOTAL);
   constexpr int B0 = MINB ? MINB : min_blocks(Layout<P, TE, false, NOB>::BATCH_TOTAL);
   constexpr int B1 = MINB ? MINB : min_blocks(Layout<P, TE, true, NOB>::BATCH_TOTAL);
   Entry e;
   e.p = P; e.te = TE; e.nt = NT; e.nob = NOB;
-  e.smem[0] = Layout<P, TE, false, NOB>::TOTAL;
-  e.smem[1] = Layout<P, TE, true, NOB>::TOTAL;
+  e.smem[0] = Layout<P, TE, false, NOB, false, true>::TOTAL;
+  e.smem[1] = Layout<P, TE, true, NOB, false, true>::TOTAL;
   e.bsmem[0] = Layout<P, TE, false, NOB>::BATCH_TOTAL;
   e.bsmem[1] = Layout<P, TE, true, NOB>::BATCH_TOTAL;
   e.fn[0] = (const void *)persist_step<P, TE, NT, false, NOB, M0, false, WE>;
@@ -91,6 +91,8 @@ int config_shape(int p, int config, int mode, TileShape *s)
   s->region_h = (e->te + 1) * p + 1;
   s->own_w = round_up(e->te * p + 2, 2);
   s->own_h = e->te * p + 1;
+  s->cell_box = e->te + 1;
+  s->minv_w = round_up(e->te * p + 1 + 4, 4);
   s->owned_buffers = (mode == MODE_DF) ? 1 : e->nob;
   s->smem = (mode == MODE_DF) ? df_smem : e->smem[mode ? 1 : 0];
   return 0;
@@ -142,8 +144,8 @@ cudaError_t launch_step(int p, int config, int mode, const CUtensorMap *maps, co
   if (mode == MODE_DF) fn = df_kernel(p, config, &smem);
   if (!fn) return cudaErrorInvalidValue;
   Params pc = prm;
-  CUtensorMap m0 = maps[0], m1 = maps[1], m2 = maps[2], m3 = maps[3];
-  void *args[] = {&m0, &m1, &m2, &m3, &pc};
+  CUtensorMap m0 = maps[0], m1 = maps[1], m2 = maps[2], m3 = maps[3], m4 = maps[4], m5 = maps[5];
+  void *args[] = {&m0, &m1, &m2, &m3, &m4, &m5, &pc};
   return cudaLaunchKernel(fn, dim3(grid), dim3(e->nt), args, smem, st);
 }
 
@@ -195,7 +197,7 @@ cudaError_t launch_record(int p, const Params &prm, cudaStream_t st, bool df)
 // tensor map of one padded float2 field, box (bw, bh) nodes
 static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 
-int make_map(CUtensorMap *map, void *base, int nx, int ny, int pitch, int bw, int bh)
+static int encoder()
 {
   if (!g_encode) {
     cudaDriverEntryPointQueryResult q;
@@ -205,12 +207,44 @@ int make_map(CUtensorMap *map, void *base, int nx, int ny, int pitch, int bw, in
       return -1;
     g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
   }
+  return 0;
+}
+
+int make_map(CUtensorMap *map, void *base, int nx, int ny, int pitch, int bw, int bh)
+{
+  if (encoder()) return -1;
   cuuint64_t dims[2] = {(cuuint64_t)nx, (cuuint64_t)ny};
   cuuint64_t strides[1] = {(cuuint64_t)pitch * 8};
   cuuint32_t box[2] = {(cuuint32_t)bw, (cuuint32_t)bh};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, base, dims, strides, box, estr,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? 0 : -(int)r - 1000;
+}
+
+int make_map_f32(CUtensorMap *map, void *base, int nx, int ny, int pitch, int bw, int bh)
+{
+  if (encoder()) return -1;
+  cuuint64_t dims[2] = {(cuuint64_t)nx, (cuuint64_t)ny};
+  cuuint64_t strides[1] = {(cuuint64_t)pitch * 4};
+  cuuint32_t box[2] = {(cuuint32_t)bw, (cuuint32_t)bh};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? 0 : -(int)r - 1000;
+}
+
+int make_map_cells(CUtensorMap *map, void *base, int mx, int my, int box)
+{
+  if (encoder()) return -1;
+  cuuint64_t dims[3] = {4, (cuuint64_t)mx, (cuuint64_t)my};
+  cuuint64_t strides[2] = {16, (cuuint64_t)mx * 16};
+  cuuint32_t bx[3] = {4, (cuuint32_t)box, (cuuint32_t)box};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, bx, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? 0 : -(int)r - 1000;
 }

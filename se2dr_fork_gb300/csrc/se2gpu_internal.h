@@ -29,7 +29,9 @@ struct se2gpu_solver {
   float *pminv, *rbuf[2];
   unsigned long long *mass_bad;  // first node with a mass that is not positive (device check at create)
   int rlast;
-  CUtensorMap maps[2][4];
+  CUtensorMap maps[2][6];        // per input buffer set: region u, cu, owned w, cw; cell constants, 1/M
+  float4 *cellc;                 // plain and Kahan modes: (lam detJ, mu detJ, d xi/dx, d eta/dy) per cell
+  int4 *tile_bounds;             // per tile: source and receiver list bounds
   int pgrid, pconfig, pntx, pnty;
   int *tile_src_off, *tile_src_idx, *tile_rec_off, *tile_rec_idx;
   std::vector<int> *src_elem_h, *rec_elem_h;

@@ -86,6 +86,20 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
       ::"r"(dst), "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar)
       : "memory");
 }
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int x, int y, int z, uint32_t bar)
+{
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(dst), "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
+// plain bulk copy (16-byte aligned addresses, a multiple of 16 bytes)
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar)
+{
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(dst), "l"((uint64_t)src), "r"(bytes), "r"(bar)
+               : "memory");
+}
 __device__ __forceinline__ void prefetch_map(const CUtensorMap *map)
 {
   asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)map) : "memory");
@@ -131,6 +145,9 @@ struct Geo {
   static constexpr int OBH = OWM;
   static constexpr int PW = OBW / 2;                      // node pairs per owned row
   static constexpr int NPAIR = OWM * PW;
+  // 1/M box (floats): the x start rounded down to a multiple of 4 (16 bytes); wide enough
+  // for the owned nodes and the paired reads' second node
+  static constexpr int MBW = round_up(OWM + 4, 4);
 };
 
 __host__ __device__ constexpr size_t al128(size_t x) { return (x + 127) & ~size_t(127); }
@@ -141,23 +158,31 @@ __host__ __device__ constexpr size_t al128(size_t x) { return (x + 127) & ~size_
 // there, and at degree 8 it fits 2 CTAs per SM instead of 1)
 __host__ __device__ constexpr int owned_buffers(int p) { return p <= 3 ? 2 : 1; }
 
-template <int P, int TE, bool KAHAN, int NOB = owned_buffers(P), bool DF = false>
+template <int P, int TE, bool KAHAN, int NOB = owned_buffers(P), bool DF = false, bool AC = false>
 struct Layout {
   typedef Geo<P, TE> G;
   static constexpr size_t REG = al128(sizeof(float2) * G::BXW * G::BXH);
   static constexpr size_t OWN = al128(sizeof(float2) * G::OBW * G::OBH);
+  // AC: the per-tile constants arrive with the copies too -- the cell constants of the
+  // tile's elements (float4 per cell) with the region, 1/M of the owned nodes and the
+  // tile's source/receiver bounds (int4) with the owned boxes
+  static constexpr size_t CELLB = AC ? al128(sizeof(float4) * G::NEX * G::NEX) : 0;
+  static constexpr size_t MINVB = AC ? al128(sizeof(float) * G::MBW * G::OBH) : 0;
+  static constexpr size_t BNDB = AC ? 128 : 0;
   // the region boxes (u and cu) are double-buffered: the next tile's arrive while this
   // tile is computed.  The owned boxes (w and cw) are read only by the node phase:
   // NOB = 2 buffers hold this tile's and the next's, NOB = 1 this tile's only.
-  static constexpr size_t STAGE = REG * (KAHAN ? 2 : 1);
-  static constexpr size_t OWNB = OWN * (KAHAN ? 2 : 1);
+  static constexpr size_t STAGE = REG * (KAHAN ? 2 : 1) + CELLB;
+  static constexpr size_t OWNB = OWN * (KAHAN ? 2 : 1) + MINVB + BNDB;
   // exchange buffer: float2 per point, float4 (two-float x, y) in the two-float mode
   static constexpr size_t XCH = al128(sizeof(float2) * (DF ? 2 : 1) * G::NE * G::XS);
   static constexpr size_t MISC = 64;
   static constexpr size_t TOTAL = 2 * STAGE + NOB * OWNB + 2 * XCH + MISC;
   static constexpr size_t BATCH_TOTAL = TOTAL;   // the batched kernel's shot parameters are a kernel parameter
-  static constexpr uint32_t TX_REGION = (uint32_t)((KAHAN ? 2 : 1) * sizeof(float2) * G::BXW * G::BXH);
-  static constexpr uint32_t TX_OWNED = (uint32_t)((KAHAN ? 2 : 1) * sizeof(float2) * G::OBW * G::OBH);
+  static constexpr uint32_t TX_REGION =
+      (uint32_t)((KAHAN ? 2 : 1) * sizeof(float2) * G::BXW * G::BXH + (AC ? sizeof(float4) * G::NEX * G::NEX : 0));
+  static constexpr uint32_t TX_OWNED =
+      (uint32_t)((KAHAN ? 2 : 1) * sizeof(float2) * G::OBW * G::OBH + (AC ? sizeof(float) * G::MBW * G::OBH + 16 : 0));
 };
 
 // CTAs per SM the register budget is sized for: as many as the shared memory allows (up
@@ -192,45 +217,68 @@ __device__ __forceinline__ TileBox tile_box(const Params &prm, int tx, int ty)
 // TMA copies of tile (tx, ty).  The box origins depend only on the tile coordinates
 // (the same formulas as tile_box); boxes reaching past the mesh read the tensor maps'
 // zero fill.  issue_region: the u (and cu) region box into a stage; issue_owned: the w
-// (and cw) owned box into the owned buffer.
-template <int P, int TE, bool KAHAN>
-__device__ __forceinline__ void issue_region(int tx, int ty, unsigned char *stage, uint32_t bar,
-                                             const CUtensorMap *tm_u, const CUtensorMap *tm_cu)
+// (and cw) owned box into the owned buffer.  AC: the cell box (tm_c: float4 per cell,
+// from the region's first element) after the region, and the 1/M box (tm_m) and the
+// tile's bounds (tb) after the owned boxes.
+template <int P, int TE, bool KAHAN, bool AC = false>
+__device__ __forceinline__ void region_boxes(int tx, int ty, unsigned char *stage, uint32_t bar,
+                                             const CUtensorMap *tm_u, const CUtensorMap *tm_cu, const CUtensorMap *tm_c)
 {
-  typedef Layout<P, TE, KAHAN> L;
+  typedef Layout<P, TE, KAHAN, 1, false, AC> L;
   const int ex0 = tx * TE, ey0 = ty * TE;
   const int RXa = (max(ex0 - 1, 0) * P) & ~1, RYa = max(ey0 - 1, 0) * P;
-  mbar_expect_tx(bar, L::TX_REGION);
   tma_load_2d(smem_u32(stage), tm_u, RXa, RYa, bar);
   if (KAHAN) tma_load_2d(smem_u32(stage + L::REG), tm_cu, RXa, RYa, bar);
+  if (AC) tma_load_3d(smem_u32(stage + L::REG * (KAHAN ? 2 : 1)), tm_c, 0, max(ex0 - 1, 0), max(ey0 - 1, 0), bar);
+}
+
+// (one arrive per barrier phase, with every byte the phase's copies bring)
+template <int P, int TE, bool KAHAN, bool AC = false>
+__device__ __forceinline__ void issue_region(int tx, int ty, unsigned char *stage, uint32_t bar,
+                                             const CUtensorMap *tm_u, const CUtensorMap *tm_cu,
+                                             const CUtensorMap *tm_c = nullptr)
+{
+  mbar_expect_tx(bar, Layout<P, TE, KAHAN, 1, false, AC>::TX_REGION);
+  region_boxes<P, TE, KAHAN, AC>(tx, ty, stage, bar, tm_u, tm_cu, tm_c);
+}
+
+template <int P, int TE, bool KAHAN, bool AC = false>
+__device__ __forceinline__ void issue_owned_boxes(int tx, int ty, unsigned char *ob, uint32_t bar,
+                                                  const CUtensorMap *tm_w, const CUtensorMap *tm_cw,
+                                                  const CUtensorMap *tm_m, const int4 *tb)
+{
+  typedef Layout<P, TE, KAHAN, 1, false, AC> L;
+  const int X0 = tx * TE * P, Y0 = ty * TE * P;
+  tma_load_2d(smem_u32(ob), tm_w, X0 & ~1, Y0, bar);
+  if (KAHAN) tma_load_2d(smem_u32(ob + L::OWN), tm_cw, X0 & ~1, Y0, bar);
+  if (AC) {
+    tma_load_2d(smem_u32(ob + L::OWN * (KAHAN ? 2 : 1)), tm_m, X0 & ~3, Y0, bar);
+    bulk_load(smem_u32(ob + L::OWN * (KAHAN ? 2 : 1) + L::MINVB), tb, 16, bar);
+  }
 }
 
 // the region and owned boxes of one tile on one barrier (two owned buffers)
-template <int P, int TE, bool KAHAN>
+template <int P, int TE, bool KAHAN, bool AC = false>
 __device__ __forceinline__ void issue_both(int tx, int ty, unsigned char *stage, unsigned char *ob, uint32_t bar,
                                            const CUtensorMap *tm_u, const CUtensorMap *tm_cu,
-                                           const CUtensorMap *tm_w, const CUtensorMap *tm_cw)
+                                           const CUtensorMap *tm_w, const CUtensorMap *tm_cw,
+                                           const CUtensorMap *tm_c = nullptr, const CUtensorMap *tm_m = nullptr,
+                                           const int4 *tb = nullptr)
 {
-  typedef Layout<P, TE, KAHAN> L;
-  const int ex0 = tx * TE, ey0 = ty * TE;
-  const int RXa = (max(ex0 - 1, 0) * P) & ~1, RYa = max(ey0 - 1, 0) * P;
-  const int OXa = (ex0 * P) & ~1, Y0 = ey0 * P;
+  typedef Layout<P, TE, KAHAN, 1, false, AC> L;
   mbar_expect_tx(bar, L::TX_REGION + L::TX_OWNED);
-  tma_load_2d(smem_u32(stage), tm_u, RXa, RYa, bar);
-  if (KAHAN) tma_load_2d(smem_u32(stage + L::REG), tm_cu, RXa, RYa, bar);
-  tma_load_2d(smem_u32(ob), tm_w, OXa, Y0, bar);
-  if (KAHAN) tma_load_2d(smem_u32(ob + L::OWN), tm_cw, OXa, Y0, bar);
+  region_boxes<P, TE, KAHAN, AC>(tx, ty, stage, bar, tm_u, tm_cu, tm_c);
+  issue_owned_boxes<P, TE, KAHAN, AC>(tx, ty, ob, bar, tm_w, tm_cw, tm_m, tb);
 }
 
-template <int P, int TE, bool KAHAN>
+template <int P, int TE, bool KAHAN, bool AC = false>
 __device__ __forceinline__ void issue_owned(int tx, int ty, unsigned char *ob, uint32_t bar,
-                                            const CUtensorMap *tm_w, const CUtensorMap *tm_cw)
+                                            const CUtensorMap *tm_w, const CUtensorMap *tm_cw,
+                                            const CUtensorMap *tm_m = nullptr, const int4 *tb = nullptr)
 {
-  typedef Layout<P, TE, KAHAN> L;
-  const int OXa = (tx * TE * P) & ~1, Y0 = ty * TE * P;
+  typedef Layout<P, TE, KAHAN, 1, false, AC> L;
   mbar_expect_tx(bar, L::TX_OWNED);
-  tma_load_2d(smem_u32(ob), tm_w, OXa, Y0, bar);
-  if (KAHAN) tma_load_2d(smem_u32(ob + L::OWN), tm_cw, OXa, Y0, bar);
+  issue_owned_boxes<P, TE, KAHAN, AC>(tx, ty, ob, bar, tm_w, tm_cw, tm_m, tb);
 }
 
 __device__ __forceinline__ void kahan_add(float &s, float &c, float inc)
@@ -275,14 +323,15 @@ struct StepPtrs {
 // one tile: prefetch of global values, wait for the tile's copies, the three
 // element phases and the node phase.  Returns false when the bounded wait expired.
 // WE: the warp-aligned item mapping (every element's lines in one warp), whose element
-// phases synchronise within the warp instead of the block
-template <int P, int TE, int NT, bool KAHAN, bool OWAIT, bool WE = false>
+// phases synchronise within the warp instead of the block.  AC: the tile's constants are
+// in shared memory, after its region and owned boxes (see Layout).
+template <int P, int TE, int NT, bool KAHAN, bool OWAIT, bool WE = false, bool AC = false>
 __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp, int tx, int ty, const unsigned char *st, uint32_t bar,
                                           uint32_t parity, const unsigned char *ob, uint32_t bar_o, uint32_t par_o,
                                           float2 *X1, float2 *X2, bool valid, int el, int j, int ecx, int ecy, float wj)
 {
   typedef Geo<P, TE> G;
-  typedef Layout<P, TE, KAHAN> L;
+  typedef Layout<P, TE, KAHAN, 1, false, AC> L;
   constexpr int N1 = G::N1, NPE = G::NPE, NEX = G::NEX, BXW = G::BXW, OBW = G::OBW, XS = G::XS;
   const float *D = c_D[P - 1];
   const float *W = c_w[P - 1];
@@ -291,17 +340,16 @@ __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp,
   const int xoff = b.EX0 * P - b.RXa;   // region-box column of the first region node
   const bool active = valid && (ecx < b.NEXa) && (ecy < b.NEYa);
   const int ex = b.EX0 + ecx, ey = b.EY0 + ecy;
-  // global loads issued before the wait: per-element constants, the tile's
-  // source/receiver list bounds and 1/M of this thread's owned node pairs
-  float lam = 0.f, mu = 0.f, ix = 0.f, iy = 0.f, detJ = 0.f;
-  if (active) {
-    const size_t cell = (size_t)ey * prm.mx + ex;
-    lam = prm.lam[cell]; mu = prm.mu[cell];
-    ix = prm.iJ00[ex]; iy = prm.iJ11[ey];
-    detJ = prm.J00[ex] * prm.J11[ey];
+  // without AC, global loads issued before the wait: the element's constants, the tile's
+  // source/receiver bounds and 1/M of this thread's owned nodes.  The barrier after the
+  // wait holds every thread until its loads in flight have landed (measured: a sixth of
+  // the step at degree 4), so with AC these arrive with the tile's copies instead.
+  float4 ccg = make_float4(0.f, 0.f, 0.f, 0.f);
+  int4 bnd = make_int4(0, 0, 0, 0);
+  if constexpr (!AC) {
+    if (active) ccg = prm.cellc[(size_t)ey * prm.mx + ex];
+    bnd = prm.tile_bounds[t];
   }
-  const int s0 = prm.tile_src_off[t], s1 = prm.tile_src_off[t + 1];
-  const int r0 = prm.tile_rec_off[t], r1 = prm.tile_rec_off[t + 1];
   // node phase granularity: pairs of adjacent nodes (16-byte accesses), or single nodes strided
   // by NT (8-byte accesses, still coalesced) when that lowers the most nodes any thread handles
   constexpr int NOWN = G::OWM * G::OWM;
@@ -312,7 +360,7 @@ __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp,
 #pragma unroll
   for (int k = 0; k < MAXS; k++) {
     minv_s[k] = 0.f;
-    if constexpr (SINGLE) {
+    if constexpr (SINGLE && !AC) {
       const int o = threadIdx.x + k * NT, oy = o / G::OWM, ox = o - (o / G::OWM) * G::OWM;
       if (o < NOWN && oy < b.OH && ox < b.OW) minv_s[k] = prm.minv[(size_t)(b.Y0 + oy) * prm.pitch + b.X0 + ox];
     }
@@ -320,7 +368,7 @@ __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp,
   float2 minv_pre[MAXP];
 #pragma unroll
   for (int k = 0; k < MAXP; k++) {
-    if constexpr (SINGLE) { minv_pre[k] = make_float2(0.f, 0.f); continue; }
+    if constexpr (SINGLE || AC) { minv_pre[k] = make_float2(0.f, 0.f); continue; }
     const int o = threadIdx.x + k * NT;
     const int oy = o / G::PW, px = o - (o / G::PW) * G::PW;
     const int XA = b.OXa + 2 * px, Y = b.Y0 + oy;
@@ -386,8 +434,11 @@ __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp,
 
   // ---- 2. stress at the row's points; xi divergence; eta fluxes to X2 ---
   if (active) {
+    // the element's (lam detJ, mu detJ, d xi/dx, d eta/dy)
+    const float4 cc = AC ? reinterpret_cast<const float4 *>(st + L::REG * (KAHAN ? 2 : 1))[ecy * NEX + ecx] : ccg;
+    const float lam = cc.x, mu = cc.y, ix = cc.z, iy = cc.w;
     const float c11 = fmaf(2.f, mu, lam);
-    const float nfj = -(detJ * wj);
+    const float nfj = -wj;
     float2 Fxi[N1];
 #pragma unroll
     for (int q = 0; q < N1; q++) {
@@ -431,6 +482,12 @@ __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp,
   } else {
     __syncthreads();   // (the owned boxes came with the region, on its barrier)
   }
+  // AC: 1/M of the owned nodes (from the column X0 rounded down to a multiple of 4) and
+  // the tile's bounds, after the owned boxes
+  const float *mbox = reinterpret_cast<const float *>(ob + L::OWN * (KAHAN ? 2 : 1));
+  if constexpr (AC) bnd = *reinterpret_cast<const int4 *>(ob + L::OWN * (KAHAN ? 2 : 1) + L::MINVB);
+  const int s0 = bnd.x, s1 = bnd.y, r0 = bnd.z, r1 = bnd.w;
+  const int MXa = b.X0 & ~3;
 
   // the node phase's parameters in registers: when prm lives in shared memory (the
   // batched kernel), every store through an output pointer would otherwise force
@@ -467,7 +524,8 @@ __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp,
           fx = fmaf(val, sv[0], fx); fy = fmaf(val, sv[1], fy);
         }
       }
-      const float2 acc = make_float2(fx * minv_s[k], fy * minv_s[k]);
+      const float mv = AC ? mbox[oy * G::MBW + (X - MXa)] : minv_s[k];
+      const float2 acc = make_float2(fx * mv, fy * mv);
       const int ri = (Y - b.RYa) * BXW + (X - b.RXa);
       const int oi = oy * OBW + (X - b.OXa);
       float2 u = rU[ri], w = oW[oi];
@@ -531,8 +589,8 @@ __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp,
         }
       }
     }
-    const float4 acc = make_float4(f[0][0] * minv_pre[k].x, f[0][1] * minv_pre[k].x,
-                                   f[1][0] * minv_pre[k].y, f[1][1] * minv_pre[k].y);
+    const float2 mv = AC ? *reinterpret_cast<const float2 *>(mbox + oy * G::MBW + (XA - MXa)) : minv_pre[k];
+    const float4 acc = make_float4(f[0][0] * mv.x, f[0][1] * mv.x, f[1][0] * mv.y, f[1][1] * mv.y);
     const int ri = (Y - b.RYa) * BXW + (XA - b.RXa);     // even: 16-byte aligned pairs
     const int oi = oy * OBW + (XA - b.OXa);
     float4 u = *reinterpret_cast<const float4 *>(rU + ri);
@@ -897,16 +955,22 @@ __device__ __forceinline__ void item_of(int &el, int &j, bool &valid)
   }
 }
 
-// DF: the two-float mode (KAHAN storage, tile_body_df); WE: the warp-aligned item mapping
+// DF: the two-float mode (KAHAN storage, tile_body_df); WE: the warp-aligned item mapping.
+// Thread 0 issues, at the start of each tile, the next tile's region (and owned boxes,
+// NOB = 2) or this tile's owned boxes (NOB = 1, on their own barrier), into the buffers
+// the previous tile freed.  Except in the two-float mode the per-tile constants come with
+// the copies (AC): the cell constants with the region, 1/M and the tile's source/receiver
+// bounds with the owned boxes.
 template <int P, int TE, int NT, bool KAHAN, int NOB = owned_buffers(P),
           int MINB = min_blocks(Layout<P, TE, KAHAN, NOB>::TOTAL), bool DF = false, bool WE = false>
 __global__ void __launch_bounds__(NT, MINB)
 persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ CUtensorMap tm_cu,
              const __grid_constant__ CUtensorMap tm_w, const __grid_constant__ CUtensorMap tm_cw,
-             const Params prm)
+             const __grid_constant__ CUtensorMap tm_c, const __grid_constant__ CUtensorMap tm_m, const Params prm)
 {
+  constexpr bool AC = !DF;   // tm_c: cell constants (float4 per cell), tm_m: 1/M
   typedef Geo<P, TE> G;
-  typedef Layout<P, TE, KAHAN, NOB, DF> L;
+  typedef Layout<P, TE, KAHAN, NOB, DF, AC> L;
   constexpr int N1 = G::N1, NEX = G::NEX;
   static_assert(WE ? NT >= 32 * G::NW : NT >= G::ITEMS, "one (element, line) item per thread");
   static_assert(NOB == 1 || NOB == 2, "one or two owned-box buffers");
@@ -929,6 +993,7 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
     fence_barrier_init();
     prefetch_map(&tm_u); prefetch_map(&tm_w);
     if (KAHAN) { prefetch_map(&tm_cu); prefetch_map(&tm_cw); }
+    if (AC) { prefetch_map(&tm_c); prefetch_map(&tm_m); }
   }
   __syncthreads();
   if (blockIdx.x == 0 && prm.record) sample_rows<P, DF>(prm, prm.rbuf_in, prm.trace_row);
@@ -943,9 +1008,10 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
   int t = blockIdx.x;
   int tx = t % prm.ntx, ty = t / prm.ntx;
   const int dtx = gridDim.x % prm.ntx, dty = gridDim.x / prm.ntx;
+  auto bnd = [&](int x, int y) { return prm.tile_bounds + (y * prm.ntx + x); };
   if (t < prm.ntiles && threadIdx.x == 0) {
-    if (NOB == 2) issue_both<P, TE, KAHAN>(tx, ty, stage0, ob0, bar0, &tm_u, &tm_cu, &tm_w, &tm_cw);
-    else issue_region<P, TE, KAHAN>(tx, ty, stage0, bar0, &tm_u, &tm_cu);
+    if (NOB == 2) issue_both<P, TE, KAHAN, AC>(tx, ty, stage0, ob0, bar0, &tm_u, &tm_cu, &tm_w, &tm_cw, &tm_c, &tm_m, bnd(tx, ty));
+    else issue_region<P, TE, KAHAN, AC>(tx, ty, stage0, bar0, &tm_u, &tm_cu, &tm_c);
   }
   for (int it = 0; t < prm.ntiles; it++, t += gridDim.x) {
     const int s = it & 1;
@@ -961,13 +1027,13 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
     const uint32_t par_o = (uint32_t)(it & 1);   // the owned barrier (one owned buffer)
     if (threadIdx.x == 0) {
       fence_proxy_async();
-      if (NOB == 1) issue_owned<P, TE, KAHAN>(tx, ty, ob0, bo0, &tm_w, &tm_cw);
+      if (NOB == 1) issue_owned<P, TE, KAHAN, AC>(tx, ty, ob0, bo0, &tm_w, &tm_cw, &tm_m, bnd(tx, ty));
       if (tn < prm.ntiles) {
         if (NOB == 2)
-          issue_both<P, TE, KAHAN>(txn, tyn, s ? stage0 : stage1, s ? ob0 : ob1, s ? bar0 : bar1, &tm_u, &tm_cu, &tm_w,
-                                   &tm_cw);
+          issue_both<P, TE, KAHAN, AC>(txn, tyn, s ? stage0 : stage1, s ? ob0 : ob1, s ? bar0 : bar1, &tm_u, &tm_cu, &tm_w,
+                                       &tm_cw, &tm_c, &tm_m, bnd(txn, tyn));
         else
-          issue_region<P, TE, KAHAN>(txn, tyn, s ? stage0 : stage1, s ? bar0 : bar1, &tm_u, &tm_cu);
+          issue_region<P, TE, KAHAN, AC>(txn, tyn, s ? stage0 : stage1, s ? bar0 : bar1, &tm_u, &tm_cu, &tm_c);
       }
     }
     bool ok;
@@ -976,9 +1042,9 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
                                              bar, parity, ob, bo0, par_o, reinterpret_cast<float4 *>(X1),
                                              reinterpret_cast<float4 *>(X2), valid, el, j, ecx, ecy);
     else
-      ok = tile_body<P, TE, NT, KAHAN, NOB == 1, WE>(prm, StepPtrs{prm.stf, prm.rbuf_out, prm.a_out}, tx, ty,
-                                                     s ? stage1 : stage0, bar, parity, ob, bo0, par_o, X1, X2, valid, el,
-                                                     j, ecx, ecy, wj);
+      ok = tile_body<P, TE, NT, KAHAN, NOB == 1, WE, AC>(prm, StepPtrs{prm.stf, prm.rbuf_out, prm.a_out}, tx, ty,
+                                                         s ? stage1 : stage0, bar, parity, ob, bo0, par_o, X1, X2, valid,
+                                                         el, j, ecx, ecy, wj);
     if (!ok) {
       if (threadIdx.x == 0) {
         atomicExch(prm.err, 1);

@@ -19,6 +19,9 @@ struct Params {
   const float *minv;               // padded, 1/M
   const float *lam, *mu;           // per cell
   const float *J00, *J11, *iJ00, *iJ11;
+  // the constants of a cell as the plain and Kahan modes use them: (lam detJ, mu detJ,
+  // d xi/dx, d eta/dy), detJ = J00 J11, each product rounded to float
+  const float4 *cellc;
   float dt, half_dt;
   float dt_lo, half_dt_lo;         // two-float mode: dt = dt + dt_lo, dt/2 = half_dt + half_dt_lo
   int nsrc;
@@ -39,10 +42,12 @@ struct Params {
   // per-tile lists (CSR over tiles) of the sources and receivers whose element
   // touches the tile's owned nodes, built on the host
   const int *tile_src_off, *tile_src_idx, *tile_rec_off, *tile_rec_idx;
+  // per tile: (first source, end of sources, first receiver, end of receivers) in the lists
+  const int4 *tile_bounds;
 };
 
 // shots per batched launch: their parameters travel in the kernel's parameter space
-// (constant bank), 96 x 288 B of the 32 KB a kernel parameter may take
+// (constant bank), 96 x 304 B of the 32 KB a kernel parameter may take
 #define SE2P_BATCH_SHOTS 96
 
 // arguments of one batched step (up to SE2P_BATCH_SHOTS shots of one degree).  A

@@ -6,8 +6,9 @@ import bench
 def test_bytes_per_node_at_degree_4():
     ne, nn = 2048 * 2048, 8193 * 8193
     cell = ne / nn
-    assert abs(bench.alg_bytes_per_node("fp32_kahan", ne, nn) - (68 + 8 * cell)) < 1e-12
-    assert abs(bench.alg_bytes_per_node("fp32", ne, nn) - (36 + 8 * cell)) < 1e-12
+    # the plain and Kahan kernels read 16 bytes of constants per cell
+    assert abs(bench.alg_bytes_per_node("fp32_kahan", ne, nn) - (68 + 16 * cell)) < 1e-12
+    assert abs(bench.alg_bytes_per_node("fp32", ne, nn) - (36 + 16 * cell)) < 1e-12
     assert abs(bench.alg_bytes_per_node("fp64", ne, nn) - (104 + 16 * cell)) < 1e-12
     # the reference's update sequence: u, v, a (+ Kahan terms of u, v) read and written, 1/M, (lambda, mu)
     assert round(bench.reference_bytes_per_node("fp32_kahan", ne, nn), 1) == 84.5
