@@ -281,6 +281,24 @@ __device__ __forceinline__ void issue_owned(int tx, int ty, unsigned char *ob, u
   issue_owned_boxes<P, TE, KAHAN, AC>(tx, ty, ob, bar, tm_w, tm_cw, tm_m, tb);
 }
 
+// the P + 1 nodes of an element row from the region box (even P: p is 16-byte aligned)
+template <int P>
+__device__ __forceinline__ void row_nodes(const float2 *p, float2 (&r)[P + 1])
+{
+  if constexpr ((P & 1) == 0) {
+#pragma unroll
+    for (int k = 0; k < P; k += 2) {
+      const float4 v = *reinterpret_cast<const float4 *>(p + k);
+      r[k] = make_float2(v.x, v.y);
+      r[k + 1] = make_float2(v.z, v.w);
+    }
+    r[P] = p[P];
+  } else {
+#pragma unroll
+    for (int k = 0; k <= P; k++) r[k] = p[k];
+  }
+}
+
 __device__ __forceinline__ void kahan_add(float &s, float &c, float inc)
 {
   const float y = inc - c;
@@ -388,15 +406,21 @@ __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp,
   const int base = (ecy * P) * BXW + ecx * P + xoff;   // region-box index of element node (0,0)
   if (active) {
     {
-      const float2 u0 = rU[base + j * BXW];
-      const float2 c0 = KAHAN ? rCU[base + j * BXW] : make_float2(0.f, 0.f);
+      // the row's nodes; at even degrees a row starts on a 16-byte boundary (xoff = 0, P and
+      // BXW even) and is read as node pairs: 8-byte reads of rows P apart would use only half
+      // of the shared-memory banks
+      float2 ur[N1], cr[N1];
+      row_nodes<P>(rU + base + j * BXW, ur);
+      if (KAHAN) row_nodes<P>(rCU + base + j * BXW, cr);
+      const float2 u0 = ur[0];
+      const float2 c0 = KAHAN ? cr[0] : make_float2(0.f, 0.f);
       float2 d[N1];
 #pragma unroll
       for (int k = 1; k < N1; k++) {
-        const float2 uk = rU[base + j * BXW + k];
+        const float2 uk = ur[k];
         d[k].x = uk.x - u0.x; d[k].y = uk.y - u0.y;
         if (KAHAN) {
-          const float2 ck = rCU[base + j * BXW + k];
+          const float2 ck = cr[k];
           d[k].x -= (ck.x - c0.x); d[k].y -= (ck.y - c0.y);
         }
       }
