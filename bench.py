@@ -45,8 +45,9 @@ def peaks():
 # DRAM bytes per node and step of the step kernels as ncu measured them (dram__bytes_read.sum +
 # dram__bytes_write.sum of one launch at 1024^2, degree 4, divided by its 16.79M nodes; the
 # kernel's traffic grows in proportion to the nodes, so it is scaled to the workload's node
-# count), from the ncu captures of the persistent FP32+Kahan step kernel at 1024^2
-MEASURED_TRAFFIC_PER_NODE = {"fp32_kahan": 1120.2e6 / 16785409}
+# count), from the ncu capture of the persistent FP32+Kahan step kernel at 1024^2 (tile
+# configuration 1: 7 x 7 elements, 320 threads, two owned buffers): 639.2 MB read + 493.6 MB written
+MEASURED_TRAFFIC_PER_NODE = {"fp32_kahan": 1132.8e6 / 16785409}
 
 
 def alg_bytes_per_node(precision: str, ne: int, nnodes: int) -> float:

@@ -47,7 +47,7 @@ struct Params {
 };
 
 // shots per batched launch: their parameters travel in the kernel's parameter space
-// (constant bank), 96 x 304 B of the 32 KB a kernel parameter may take
+// (constant bank), 96 x 312 B of the 32 KB a kernel parameter may take
 #define SE2P_BATCH_SHOTS 96
 
 // arguments of one batched step (up to SE2P_BATCH_SHOTS shots of one degree).  A
