@@ -334,25 +334,30 @@ def run_ours(args, rank, world):
                 "peak_kind": "measured (se2gpu_pipe_peak %s)" % kind,
                 "note": "algorithmic arithmetic operations per node (no halo recompute) x nodes / step time"}
 
-    # end to end through the C-ABI: create (upload from host) + K steps + traces read back + destroy
+    # end to end through the C-ABI: create (upload from host) + K steps + traces read back +
+    # destroy, three times (each a complete job); the median job is reported, every run listed
     prec = args.precision
-    barrier()
-    t0 = time.perf_counter()
-    sol = G.Solver(setup, prec, trace_capacity=args.steps + 2)
-    if prec != "fp64":
-        if args.tile_config >= 0:
-            sol.set_tile_config(args.tile_config)
-        else:
-            autotune.apply(sol, prec)
-    t_create = time.perf_counter()
-    sol.advance(args.steps)
-    tr = sol.traces()
-    t_steps = time.perf_counter()
-    sol.close()
-    torch.cuda.synchronize()
-    t_end = time.perf_counter()
-    e2e_s = tmax(t_end - t0)
-    e2e_parts = {"create_s": t_create - t0, "steps_and_traces_s": t_steps - t_create, "destroy_s": t_end - t_steps}
+    runs = []
+    for _ in range(3):
+        barrier()
+        t0 = time.perf_counter()
+        sol = G.Solver(setup, prec, trace_capacity=args.steps + 2)
+        if prec != "fp64":
+            if args.tile_config >= 0:
+                sol.set_tile_config(args.tile_config)
+            else:
+                autotune.apply(sol, prec)
+        t_create = time.perf_counter()
+        sol.advance(args.steps)
+        tr = sol.traces()
+        t_steps = time.perf_counter()
+        sol.close()
+        torch.cuda.synchronize()
+        t_end = time.perf_counter()
+        runs.append((tmax(t_end - t0), {"create_s": t_create - t0, "steps_and_traces_s": t_steps - t_create,
+                                        "destroy_s": t_end - t_steps}))
+    e2e_s, e2e_parts = sorted(runs, key=lambda r: r[0])[1]
+    e2e_runs = [r[0] for r in runs]
     # bytes of the caller's FP64 host arrays that se2gpu_create and advance read: the mass, the
     # cell Lame parameters, the Jacobians, D and the weights, the source values, the receiver
     # indices and the STF values of every step (the FP32 modes convert on the device)
@@ -390,6 +395,7 @@ def run_ours(args, rank, world):
             "tile": head.get("tile"), "autotune": tuned,
             "e2e": {"value": world * dof * args.steps / e2e_s, "unit": "DOF/s", "h2d_bytes_per_step": h2d / args.steps,
                     "d2h_bytes_per_step": d2h / args.steps, "seconds": e2e_s, "parts": e2e_parts,
+                    "runs_s": e2e_runs, "of_runs": "median of 3 complete jobs",
                     "includes": "se2gpu_create (upload of the set-up from host memory), advance, traces, destroy"},
             "cpu_baseline": cpu}
     for leg in ("fp64", "fp32_df"):

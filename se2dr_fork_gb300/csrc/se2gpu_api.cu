@@ -354,6 +354,8 @@ extern "C" void se2gpu_destroy(se2gpu_solver *h)
 {
   if (!h) return;
   cudaSetDevice(h->device);
+  for (cudaEvent_t &ev : h->side_done)   // set-up work of a create that failed part-way
+    if (ev) { cudaEventSynchronize(ev); cudaEventDestroy(ev); ev = nullptr; }
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (int b = 0; b < 2; b++) {
     for (int f = 0; f < 3; f++) dfree(h, h->f64[b][f]);
@@ -623,8 +625,53 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
           (const float *)h->iJ00, (const float *)h->iJ11, h->mx, ne, h->cellc);
       if (cudaGetLastError() != cudaSuccess) { fail(h, SE2GPU_ERR_CUDA, "cell constants"); TRY(SE2GPU_ERR_CUDA); }
     }
-    // the step kernel's tables and tile configuration first: their small uploads then wait
-    // only for the cell tables above, not for the clearing and the 1/M pass below
+    // The fields start at zero: the first buffer set and a are cleared.  The second set is
+    // written at every mesh node by the first step before anything reads it (the tile copies
+    // never read past the mesh), so only its row padding is cleared, to keep checkpoints
+    // deterministic.  The clearing and, on a device that reads pageable host memory, the 1/M
+    // pass over the caller's mass (the longest part of the set-up: it runs at the host link's
+    // rate) run on two side streams, beside the host's tile configuration below; the handle's
+    // stream joins them after it, so the configuration's small uploads wait only for the cell
+    // tables above.
+    if (h->pageable) {
+      TRY(dalloc(h, (void **)&h->pminv, np * 4 * (df ? 2 : 1)));
+      TRY(dalloc(h, (void **)&h->mass_bad, sizeof(unsigned long long)));
+    }
+    {
+      cudaStream_t side[2] = {nullptr, nullptr};
+      cudaEvent_t ev0 = nullptr;
+      cudaError_t e = cudaEventCreateWithFlags(&ev0, cudaEventDisableTiming);
+      for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+        e = cudaStreamCreateWithFlags(&side[i], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->side_done[i], cudaEventDisableTiming);
+      }
+      if (e == cudaSuccess) e = cudaEventRecord(ev0, h->stream);   // the allocations above
+      for (int i = 0; i < 2 && e == cudaSuccess; i++) e = cudaStreamWaitEvent(side[i], ev0, 0);
+      float2 *full[5] = {h->pu[0], h->pw[0], kahan ? h->pcu[0] : nullptr, kahan ? h->pcw[0] : nullptr, h->pa};
+      for (int f = 0; f < 5 && e == cudaSuccess; f++)
+        if (full[f]) e = cudaMemsetAsync(full[f], 0, np * 8 * ((f == 4 && df) ? 2 : 1), side[0]);
+      float2 *pad[4] = {h->pu[1], h->pw[1], kahan ? h->pcu[1] : nullptr, kahan ? h->pcw[1] : nullptr};
+      for (int f = 0; f < 4 && e == cudaSuccess; f++)
+        if (pad[f]) e = cudaMemset2DAsync(pad[f] + nx_g, (size_t)h->pitch * 8, 0, (size_t)(h->pitch - nx_g) * 8, ny_g, side[0]);
+      if (h->pageable && e == cudaSuccess) {
+        // the device reads the mass where it lies (no staging copy of the whole array)
+        e = cudaMemsetAsync(h->mass_bad, 0xff, sizeof(unsigned long long), side[1]);
+        if (e == cudaSuccess) {
+          k_minv_from_host<<<dim3((h->pitch + 1023) / 1024, (unsigned)std::min(ny_g, 65535L)), 256, 0, side[1]>>>(
+              P->mass, nx_g, ny_g, h->pitch, h->pminv, df ? h->pminv + np : nullptr, h->mass_bad);
+          e = cudaGetLastError();
+        }
+      }
+      for (int i = 0; i < 2 && e == cudaSuccess; i++) e = cudaEventRecord(h->side_done[i], side[i]);
+      if (ev0) cudaEventDestroy(ev0);
+      for (int i = 0; i < 2; i++)
+        if (side[i]) cudaStreamDestroy(side[i]);   // released once its work is done
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        fail(h, SE2GPU_ERR_CUDA, "clearing the state and 1/M: %s", cudaGetErrorString(e));
+        TRY(SE2GPU_ERR_CUDA);
+      }
+    }
     {
       cudaError_t e = se2p::set_tables(P->p, P->D, P->w1d);
       if (e != cudaSuccess) { fail(h, SE2GPU_ERR_CUDA, "constant tables: %s", cudaGetErrorString(e)); TRY(SE2GPU_ERR_CUDA); }
@@ -632,51 +679,13 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
       h->rec_elem_h = new std::vector<int>(P->rec_elem, P->rec_elem + P->nrec);
       TRY(setup_f32_config(h, 0, true));
     }
-    // The fields start at zero: the first buffer set and a are cleared.  The second set is
-    // written at every mesh node by the first step before anything reads it (the tile copies
-    // never read past the mesh), so only its row padding is cleared, to keep checkpoints
-    // deterministic.  The clearing runs on a second stream, beside the kernels below that
-    // read the caller's arrays over the host link, and the handle's stream waits for it.
-    {
-      cudaStream_t side = nullptr;
-      cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-      cudaError_t e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
-      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev0, cudaEventDisableTiming);
-      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev1, cudaEventDisableTiming);
-      if (e == cudaSuccess) e = cudaEventRecord(ev0, h->stream);   // the allocations above
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(side, ev0, 0);
-      float2 *full[5] = {h->pu[0], h->pw[0], kahan ? h->pcu[0] : nullptr, kahan ? h->pcw[0] : nullptr, h->pa};
-      for (int f = 0; f < 5 && e == cudaSuccess; f++)
-        if (full[f]) e = cudaMemsetAsync(full[f], 0, np * 8 * ((f == 4 && df) ? 2 : 1), side);
-      float2 *pad[4] = {h->pu[1], h->pw[1], kahan ? h->pcu[1] : nullptr, kahan ? h->pcw[1] : nullptr};
-      for (int f = 0; f < 4 && e == cudaSuccess; f++)
-        if (pad[f]) e = cudaMemset2DAsync(pad[f] + nx_g, (size_t)h->pitch * 8, 0, (size_t)(h->pitch - nx_g) * 8, ny_g, side);
-      if (e == cudaSuccess) e = cudaEventRecord(ev1, side);
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, ev1, 0);
-      if (ev0) cudaEventDestroy(ev0);
-      if (ev1) cudaEventDestroy(ev1);
-      if (side) cudaStreamDestroy(side);   // released once its work is done
-      if (e != cudaSuccess) {
-        cudaGetLastError();
-        fail(h, SE2GPU_ERR_CUDA, "clearing the state: %s", cudaGetErrorString(e));
-        TRY(SE2GPU_ERR_CUDA);
-      }
+    for (cudaEvent_t &ev : h->side_done) {
+      const cudaError_t e = cudaStreamWaitEvent(h->stream, ev, 0);
+      cudaEventDestroy(ev);   // (the wait keeps what it needs)
+      ev = nullptr;
+      if (e != cudaSuccess) { cudaGetLastError(); fail(h, SE2GPU_ERR_CUDA, "joining the set-up streams"); TRY(SE2GPU_ERR_CUDA); }
     }
-    if (h->pageable) {
-      // the device reads the mass where it lies (no staging copy of the whole array)
-      TRY(dalloc(h, (void **)&h->pminv, np * 4 * (df ? 2 : 1)));
-      TRY(dalloc(h, (void **)&h->mass_bad, sizeof(unsigned long long)));
-      if (cudaMemsetAsync(h->mass_bad, 0xff, sizeof(unsigned long long), h->stream) != cudaSuccess) {
-        fail(h, SE2GPU_ERR_CUDA, "mass check set-up");
-        TRY(SE2GPU_ERR_CUDA);
-      }
-      k_minv_from_host<<<dim3((h->pitch + 1023) / 1024, (unsigned)std::min(ny_g, 65535L)), 256, 0, h->stream>>>(
-          P->mass, nx_g, ny_g, h->pitch, h->pminv, df ? h->pminv + np : nullptr, h->mass_bad);
-      if (cudaGetLastError() != cudaSuccess) {
-        fail(h, SE2GPU_ERR_CUDA, "1/M from host memory");
-        TRY(SE2GPU_ERR_CUDA);
-      }
-    } else {
+    if (!h->pageable) {
       // 1/M in the padded FP32 layout (padding nodes 0), row blocks on the host threads;
       // the two-float mode appends the remainders
       const size_t nm = np * (df ? 2 : 1);

@@ -28,6 +28,7 @@ struct se2gpu_solver {
   float2 *pu[2], *pw[2], *pcu[2], *pcw[2], *pa;
   float *pminv, *rbuf[2];
   unsigned long long *mass_bad;  // first node with a mass that is not positive (device check at create)
+  cudaEvent_t side_done[2];      // se2gpu_create: set-up work on side streams not yet joined
   int rlast;
   CUtensorMap maps[2][6];        // per input buffer set: region u, cu, owned w, cw; cell constants, 1/M
   float4 *cellc;                 // plain and Kahan modes: (lam detJ, mu detJ, d xi/dx, d eta/dy) per cell
