@@ -133,9 +133,13 @@ int se2gpu_device_fields(const se2gpu_solver *h, void **u, void **v, void **a);
 
 /* Tile configurations of the step kernel (elements per tile edge, threads per
    CTA) available for the handle's degree and precision, for the autotuner;
-   returns how many exist.  se2gpu_set_tile_config selects one (default 0). */
+   returns how many exist.  se2gpu_set_tile_config selects one; se2gpu_tile_config
+   returns the selected one (a new handle starts with the configuration measured
+   fastest for its degree on GB300 in the plain and Kahan modes, 0 in the two-float
+   and FP64 modes). */
 int se2gpu_tile_configs(const se2gpu_solver *h, int *edge, int *threads, int max_configs);
 int se2gpu_set_tile_config(se2gpu_solver *h, int config);
+int se2gpu_tile_config(const se2gpu_solver *h);
 /* One configuration in full (no counterpart in the reference): info = {elements per
    tile edge, threads per CTA, owned-box buffers (2: the next tile's w arrives a tile
    ahead; 1: during the tile's element phases; 0: FP64), resident CTAs per SM on the

@@ -677,7 +677,7 @@ extern "C" int se2gpu_create(const se2gpu_problem *P, int precision, int trace_c
       if (e != cudaSuccess) { fail(h, SE2GPU_ERR_CUDA, "constant tables: %s", cudaGetErrorString(e)); TRY(SE2GPU_ERR_CUDA); }
       h->src_elem_h = new std::vector<int>(P->src_elem, P->src_elem + P->nsrc);
       h->rec_elem_h = new std::vector<int>(P->rec_elem, P->rec_elem + P->nrec);
-      TRY(setup_f32_config(h, 0, true));
+      TRY(setup_f32_config(h, df ? 0 : se2p::default_config(P->p), true));
     }
     for (cudaEvent_t &ev : h->side_done) {
       const cudaError_t e = cudaStreamWaitEvent(h->stream, ev, 0);
@@ -1161,6 +1161,12 @@ extern "C" int se2gpu_tile_config_info(const se2gpu_solver *h, int config, int i
   }
   info[3] = se2p::occupancy(h->p, config, pmode(h), false);
   return 0;
+}
+
+extern "C" int se2gpu_tile_config(const se2gpu_solver *h)
+{
+  if (!h) return SE2GPU_ERR_ARG;
+  return is_f64(h) ? 0 : h->pconfig;
 }
 
 extern "C" int se2gpu_set_tile_config(se2gpu_solver *h, int config)

@@ -71,6 +71,14 @@ static const Entry *find(int p, int config)
   return nullptr;
 }
 
+// the configuration a handle starts with: per degree the one the autotuner measured
+// fastest on GB300 at about 16M nodes (and, at degree 4, at the 2048^2 workload)
+int default_config(int p)
+{
+  static const int best[8] = {2, 0, 2, 1, 2, 0, 2, 1};
+  return (p >= 1 && p <= 8 && best[p - 1] < num_configs(p)) ? best[p - 1] : 0;
+}
+
 int num_configs(int p)
 {
   int n, k = 0;

@@ -41,6 +41,7 @@ struct TileShape {
 
 cudaError_t set_tables(int p, const double *D, const double *w1d);   // constant-memory D, w (current device)
 int num_configs(int p);                                               // tile configurations for degree p
+int default_config(int p);                                            // a new handle's (plain and Kahan modes)
 // mode: MODE_PLAIN, MODE_KAHAN or MODE_DF (the batched kernel: plain or Kahan)
 int config_shape(int p, int config, int mode, TileShape *s);
 cudaError_t prepare(int p, int config, int mode);                     // dynamic shared-memory limit

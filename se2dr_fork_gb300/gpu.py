@@ -25,6 +25,7 @@ EXPORTS = ["se2gpu_create", "se2gpu_destroy", "se2gpu_last_error", "se2gpu_creat
            "se2gpu_synchronize", "se2gpu_selftest_wait_expiry", "se2gpu_set_fields", "se2gpu_get_fields", "se2gpu_advance", "se2gpu_traces",
            "se2gpu_norms", "se2gpu_assemble_linear_form", "se2gpu_assemble_linear_form_device", "se2gpu_info",
            "se2gpu_device_fields", "se2gpu_tile_configs", "se2gpu_tile_config_info", "se2gpu_set_tile_config",
+           "se2gpu_tile_config",
            "se2gpu_ensemble_create", "se2gpu_ensemble_destroy", "se2gpu_ensemble_last_error",
            "se2gpu_ensemble_set_stream", "se2gpu_ensemble_set_graphs", "se2gpu_ensemble_set_tile_config",
            "se2gpu_ensemble_tile_config", "se2gpu_ensemble_advance", "se2gpu_ensemble_enqueue",
@@ -89,6 +90,7 @@ def lib():
         L.se2gpu_tile_configs.argtypes = [vp, _ip, _ip, C.c_int]
         L.se2gpu_tile_config_info.argtypes = [vp, C.c_int, _ip]
         L.se2gpu_set_tile_config.argtypes = [vp, C.c_int]
+        L.se2gpu_tile_config.argtypes = [vp]
         L.se2gpu_ensemble_create.argtypes = [C.POINTER(_CProblem), C.c_int, C.c_int, C.c_int, C.POINTER(vp)]
         L.se2gpu_ensemble_destroy.argtypes = [vp]
         L.se2gpu_ensemble_destroy.restype = None
@@ -157,7 +159,7 @@ class Solver:
         if rc != 0:
             raise GpuError(f"se2gpu_create failed ({rc}): {lib().se2gpu_create_error().decode()}")
         self._h = h
-        self.tile_config = 0
+        self.tile_config = self._check(lib().se2gpu_tile_config(h), "se2gpu_tile_config")
         self.time = 0.0
         self.step = 0
         self._times = []

@@ -343,6 +343,21 @@ def test_fp32_tile_configs_agree_many_tiles_per_cta(precision):
             assert all(np.array_equal(x, y) for x, y in zip(out, ref)), c
 
 
+def test_default_tile_config_and_getter():
+    """A new plain or Kahan handle starts with its degree's default configuration (degree 4:
+    configuration 1, 7x7 tiles with two owned buffers); the two-float and FP64 modes with 0;
+    se2gpu_tile_config follows se2gpu_set_tile_config."""
+    setup = H.Setup(S.demo(9, 7, p=4, tmax=1.0).replace(nt=4))
+    for prec, want in [("fp32_kahan", 1), ("fp32", 1), ("fp32_df", 0), ("fp64", 0)]:
+        sol = G.Solver(setup, prec)
+        assert sol.tile_config == want, prec
+        assert G.lib().se2gpu_tile_config(sol._h) == want
+        if prec != "fp64":
+            sol.set_tile_config(2)
+            assert G.lib().se2gpu_tile_config(sol._h) == 2
+        sol.close()
+
+
 @pytest.mark.parametrize("p", [1, 3, 4, 8])
 def test_tile_config_info(p):
     """se2gpu_tile_config_info agrees with se2gpu_tile_configs and reports one or two owned
