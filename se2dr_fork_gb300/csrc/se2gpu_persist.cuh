@@ -152,10 +152,10 @@ struct Geo {
 
 __host__ __device__ constexpr size_t al128(size_t x) { return (x + 127) & ~size_t(127); }
 
-// owned-box buffers per degree (the default of the tile configurations): 2 up to degree
-// 3 (the next tile's w, cw arrive with its region, a whole tile ahead), 1 above (the
-// current tile's arrive during its element phases; the smaller footprint is faster
-// there, and at degree 8 it fits 2 CTAs per SM instead of 1)
+// owned-box buffers of the tile configurations that name none: 2 up to degree 3 (the
+// next tile's w, cw arrive with its region, a whole tile ahead), 1 above (the current
+// tile's arrive during its element phases; the smaller footprint fits 2 CTAs per SM at
+// degree 8 instead of 1).  Degree 4 runs fastest with two (its configuration 1).
 __host__ __device__ constexpr int owned_buffers(int p) { return p <= 3 ? 2 : 1; }
 
 template <int P, int TE, bool KAHAN, int NOB = owned_buffers(P), bool DF = false, bool AC = false>

@@ -12,11 +12,12 @@ namespace se2p {
 // sized for (0: as many as the shared memory allows, up to 3), item mapping (0: one
 // thread per (element, line) in order, threads >= (edge + 1)^2 (degree + 1); 1:
 // warp-aligned, 32 / (degree + 1) whole elements per warp, whose three element phases
-// synchronise within the warp, threads = 32 x warps)).  Degree 4: 7x7 with one owned
-// buffer kept at 2 CTAs per SM (92 registers) is the fastest in order mapping; sized for
-// 3 CTAs it is capped at 64 registers and runs slower.  The two-float mode uses the same
-// list with one owned buffer.  New configurations go at the end of their degree's list:
-// the autotuner's cache refers to them by position.
+// synchronise within the warp, threads = 32 x warps)).  Degree 4: 7x7 at 2 CTAs per SM
+// (92-96 registers) is the fastest, with two owned buffers; sized for 3 CTAs it is capped
+// at 64 registers and runs slower.  default_config gives each degree's fastest.  The
+// two-float mode uses the same list with one owned buffer.  New configurations go at the
+// end of their degree's list: the autotuner's cache and default_config refer to them by
+// position.
 #define SE2P_CONFIGS(X)                                                                      \
   X(1, 15, 512, 0, 0, 0) X(1, 11, 288, 0, 0, 0) X(1, 15, 512, 0, 0, 1)                       \
   X(2, 12, 512, 2, 2, 0) X(2, 10, 384, 0, 0, 0) X(2, 8, 256, 0, 0, 0) X(2, 10, 416, 0, 0, 1) \
