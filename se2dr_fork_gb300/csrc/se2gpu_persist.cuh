@@ -129,6 +129,12 @@ struct Geo {
   // element would start on bank 0; pads chosen with a wavefront model of the kernel's
   // accesses)
   static constexpr int XS = NPE + (P == 1 ? 2 : P == 3 ? 3 : P == 6 ? 6 : P == 7 ? 7 : P == 8 ? 8 : 0);
+  // the plain and Kahan tile body's exchange buffers: element stride XSK and the stride RS of
+  // an element's rows (point (a, b) at a + b RS).  At degree 4 rows of 6 in elements of 37
+  // float2: the same wavefront count gives 9-10 % fewer exchange-buffer wavefronts than
+  // rows of 5 in elements of 25 for 6x6, 7x7 and 8x8 tiles (the two-float body keeps XS)
+  static constexpr int RS = (P == 4) ? 6 : N1;
+  static constexpr int XSK = (P == 4) ? 37 : XS;
   static constexpr int NEX = TE + 1, NE = NEX * NEX;      // elements incl. halo
   static constexpr int ITEMS = NE * N1;                   // (element, line) work items
   // warp-aligned mapping: EPW whole elements per warp (their N1 lines in consecutive
@@ -175,7 +181,7 @@ struct Layout {
   static constexpr size_t STAGE = REG * (KAHAN ? 2 : 1) + CELLB;
   static constexpr size_t OWNB = OWN * (KAHAN ? 2 : 1) + MINVB + BNDB;
   // exchange buffer: float2 per point, float4 (two-float x, y) in the two-float mode
-  static constexpr size_t XCH = al128(sizeof(float2) * (DF ? 2 : 1) * G::NE * G::XS);
+  static constexpr size_t XCH = al128(DF ? sizeof(float4) * G::NE * G::XS : sizeof(float2) * G::NE * G::XSK);
   static constexpr size_t MISC = 64;
   static constexpr size_t TOTAL = 2 * STAGE + NOB * OWNB + 2 * XCH + MISC;
   static constexpr size_t BATCH_TOTAL = TOTAL;   // the batched kernel's shot parameters are a kernel parameter
@@ -350,7 +356,7 @@ __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp,
 {
   typedef Geo<P, TE> G;
   typedef Layout<P, TE, KAHAN, 1, false, AC> L;
-  constexpr int N1 = G::N1, NPE = G::NPE, NEX = G::NEX, BXW = G::BXW, OBW = G::OBW, XS = G::XS;
+  constexpr int N1 = G::N1, NPE = G::NPE, NEX = G::NEX, BXW = G::BXW, OBW = G::OBW, XS = G::XSK, RS = G::RS;
   const float *D = c_D[P - 1];
   const float *W = c_w[P - 1];
   const TileBox b = tile_box<P, TE>(prm, tx, ty);
@@ -450,7 +456,7 @@ __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp,
         float sx = 0.f, sy = 0.f;
 #pragma unroll
         for (int k = 1; k < N1; k++) { sx = fmaf(D[q * N1 + k], d[k].x, sx); sy = fmaf(D[q * N1 + k], d[k].y, sy); }
-        X1[el * XS + j + q * N1] = make_float2(sx, sy);   // d/deta at (j, q)
+        X1[el * XS + j + q * RS] = make_float2(sx, sy);   // d/deta at (j, q)
       }
     }
   }
@@ -466,13 +472,13 @@ __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp,
     float2 Fxi[N1];
 #pragma unroll
     for (int q = 0; q < N1; q++) {
-      const float2 ge = X1[el * XS + q + j * N1];   // d/deta at (q, j)
+      const float2 ge = X1[el * XS + q + j * RS];   // d/deta at (q, j)
       const float e0 = ix * gxi[q].x, e1 = iy * ge.y, e2 = fmaf(ix, gxi[q].y, iy * ge.x);
       const float nf = nfj * W[q];                   // -detJ w_q w_j
       const float fx_ = ix * nf, fy_ = iy * nf;
       const float sxx = fmaf(c11, e0, lam * e1), syy = fmaf(lam, e0, c11 * e1), sxy = mu * e2;
       Fxi[q] = make_float2(fx_ * sxx, fx_ * sxy);
-      X2[el * XS + q + j * N1] = make_float2(fy_ * sxy, fy_ * syy);
+      X2[el * XS + q + j * RS] = make_float2(fy_ * sxy, fy_ * syy);
     }
     // xi part of the divergence for the row's nodes, to X1 (this thread alone read row j of X1)
 #pragma unroll
@@ -480,7 +486,7 @@ __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp,
       float rx = 0.f, ry = 0.f;
 #pragma unroll
       for (int q = 0; q < N1; q++) { rx = fmaf(D[q * N1 + a], Fxi[q].x, rx); ry = fmaf(D[q * N1 + a], Fxi[q].y, ry); }
-      X1[el * XS + a + j * N1] = make_float2(rx, ry);
+      X1[el * XS + a + j * RS] = make_float2(rx, ry);
     }
   }
   if constexpr (WE) __syncwarp(); else __syncthreads();
@@ -489,14 +495,14 @@ __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp,
   if (active) {
     float2 fc[N1];
 #pragma unroll
-    for (int q = 0; q < N1; q++) fc[q] = X2[el * XS + j + q * N1];
+    for (int q = 0; q < N1; q++) fc[q] = X2[el * XS + j + q * RS];
 #pragma unroll
     for (int bq = 0; bq < N1; bq++) {
-      const float2 r = X1[el * XS + j + bq * N1];
+      const float2 r = X1[el * XS + j + bq * RS];
       float cx = r.x, cy = r.y;
 #pragma unroll
       for (int q = 0; q < N1; q++) { cx = fmaf(D[q * N1 + bq], fc[q].x, cx); cy = fmaf(D[q * N1 + bq], fc[q].y, cy); }
-      X1[el * XS + j + bq * N1] = make_float2(cx, cy);
+      X1[el * XS + j + bq * RS] = make_float2(cx, cy);
     }
   }
   if (OWAIT) {
@@ -533,9 +539,9 @@ __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp,
         const int ex = lx / P, ey = ly / P, ix = lx - ex * P, iy = ly - ey * P;
         const bool in_x = X < NXP, in_y = Y < NYP;
         const bool lft = (ix == 0) && (X > 0), bot = (iy == 0) && (Y > 0);
-        const int own = (ey * NEX + ex) * XS + ix + iy * N1;
-        if (bot && lft) { const float2 fe = X1[own - NEX * XS - XS + P + P * N1]; fx += fe.x; fy += fe.y; }
-        if (bot && in_x) { const float2 fe = X1[own - NEX * XS + P * N1]; fx += fe.x; fy += fe.y; }
+        const int own = (ey * NEX + ex) * XS + ix + iy * RS;
+        if (bot && lft) { const float2 fe = X1[own - NEX * XS - XS + P + P * RS]; fx += fe.x; fy += fe.y; }
+        if (bot && in_x) { const float2 fe = X1[own - NEX * XS + P * RS]; fx += fe.x; fy += fe.y; }
         if (lft && in_y) { const float2 fe = X1[own - XS + P]; fx += fe.x; fy += fe.y; }
         if (in_x && in_y) { const float2 fe = X1[own]; fx += fe.x; fy += fe.y; }
       }
@@ -598,9 +604,9 @@ __device__ __forceinline__ bool tile_body(const Params &prm, const StepPtrs stp,
       const int ex = lx / P, ey = ly / P, ix = lx - ex * P, iy = ly - ey * P;
       const bool in_x = X < NXP, in_y = Y < NYP;
       const bool lft = (ix == 0) && (X > 0), bot = (iy == 0) && (Y > 0);
-      const int own = (ey * NEX + ex) * XS + ix + iy * N1;
-      if (bot && lft) { const float2 fe = X1[own - NEX * XS - XS + P + P * N1]; f[h][0] += fe.x; f[h][1] += fe.y; }
-      if (bot && in_x) { const float2 fe = X1[own - NEX * XS + P * N1]; f[h][0] += fe.x; f[h][1] += fe.y; }
+      const int own = (ey * NEX + ex) * XS + ix + iy * RS;
+      if (bot && lft) { const float2 fe = X1[own - NEX * XS - XS + P + P * RS]; f[h][0] += fe.x; f[h][1] += fe.y; }
+      if (bot && in_x) { const float2 fe = X1[own - NEX * XS + P * RS]; f[h][0] += fe.x; f[h][1] += fe.y; }
       if (lft && in_y) { const float2 fe = X1[own - XS + P]; f[h][0] += fe.x; f[h][1] += fe.y; }
       if (in_x && in_y) { const float2 fe = X1[own]; f[h][0] += fe.x; f[h][1] += fe.y; }
       for (int q = s0; q < s1; q++) {
