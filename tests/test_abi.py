@@ -173,3 +173,16 @@ def test_noalloc_norms_reject_bad_lengths_without_gpu(gpu_lib, n, msg):
     assert msg in gpu.lib().se2gpu_last_error(None)
     assert gpu.lib().se2gpu_norms_device_noalloc(None, ctypes.c_void_p(512), 10, None, out) == -1
     assert b"null argument" in gpu.lib().se2gpu_last_error(None)
+
+
+def test_tile_configuration_queries_reject_a_null_handle_without_gpu(gpu_lib):
+    """The tile-configuration entry points return SE2GPU_ERR_ARG (-1) for a null handle
+    before any device call (se2gpu_tile_config included)."""
+    from se2dr_fork_gb300 import gpu
+    L = gpu.lib()
+    info = (ctypes.c_int * 4)()
+    e = (ctypes.c_int * 4)()
+    assert L.se2gpu_tile_config(None) == -1
+    assert L.se2gpu_set_tile_config(None, 0) == -1
+    assert L.se2gpu_tile_configs(None, e, e, 4) == -1
+    assert L.se2gpu_tile_config_info(None, 0, info) == -1
