@@ -1001,7 +1001,7 @@ persist_step(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ C
   constexpr bool AC = !DF;   // tm_c: cell constants (float4 per cell), tm_m: 1/M
   typedef Geo<P, TE> G;
   typedef Layout<P, TE, KAHAN, NOB, DF, AC> L;
-  constexpr int N1 = G::N1, NEX = G::NEX;
+  constexpr int NEX = G::NEX;
   static_assert(WE ? NT >= 32 * G::NW : NT >= G::ITEMS, "one (element, line) item per thread");
   static_assert(NOB == 1 || NOB == 2, "one or two owned-box buffers");
   static_assert(!DF || (KAHAN && NOB == 1), "the two-float mode keeps the Kahan storage and one owned buffer");
@@ -1110,7 +1110,7 @@ persist_batch(const __grid_constant__ BatchArgs ba)
 {
   typedef Geo<P, TE> G;
   typedef Layout<P, TE, KAHAN, NOB> L;
-  constexpr int N1 = G::N1, NEX = G::NEX;
+  constexpr int NEX = G::NEX;
   static_assert(WE ? NT >= 32 * G::NW : NT >= G::ITEMS, "one (element, line) item per thread");
   static_assert(NOB == 1 || NOB == 2, "one or two owned-box buffers");
   const float *W = c_w[P - 1];
