@@ -35,3 +35,9 @@ def test_clock_summary_reports_median_and_slowdowns():
     c.lines.append("0, 1200, 2070, 700, 0x8, Active, Not Active, Not Active, Not Active")
     assert "hw_slowdown" in c.summary()["reasons"]
     assert bench.ClockSampler(0).summary()["sm_mhz"] is None
+
+
+def test_median_job_reports_the_middle_run_with_its_parts():
+    runs = [(0.0516, {"create_s": 0.0516}), (0.0243, {"create_s": 0.0042}), (0.0244, {"create_s": 0.0043})]
+    assert bench.median_job(runs) == (0.0244, {"create_s": 0.0043})
+    assert bench.median_job(runs[:1]) == runs[0]
